@@ -1,0 +1,301 @@
+"""GRG matmul benchmark (edge x K updates per second, and the HBM roofline of the sweep kernel).
+
+Workload (default): the seeded window-tree GRG with N=200,000 haplotypes and M=1,000,000 variants
+(seed 42, 100-variant windows), plain single-request matmul in both directions for
+K in {1, 8, 32, 64} and dtypes int32 (0/1 genotype counts), float32 (compensated) and float64
+(N(0,1) inputs).  One step = those 24 matmuls.  `value` = sum of E*K over the step's matmuls /
+device time, inputs resident in HBM; `e2e` = the same through the host-buffer C-ABI path, with
+every input copied in and every output copied back inside the timed region.
+
+    python bench.py [--gpus 1] [--steps 5] [--warmup 3] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+DOWN, UP = 1, 2
+METRIC = "GRG matmul edge*K updates/s"
+UNIT = "edge*K/s"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="grgx", choices=["grgx", "reference"])
+    ap.add_argument("--samples", type=int, default=200_000)
+    ap.add_argument("--mutations", type=int, default=1_000_000)
+    ap.add_argument("--seed", type=int, default=42)
+    ap.add_argument("--ks", default="1,8,32,64")
+    ap.add_argument("--dtypes", default="int32,float32,float64")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline sample budget")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def workload(args):
+    ks = [int(k) for k in args.ks.split(",")]
+    dts = [np.dtype(d) for d in args.dtypes.split(",")]
+    return [(dt, K, d) for dt in dts for K in ks for d in (UP, DOWN)]
+
+
+def make_inputs(rng, combos, N, M):
+    out = []
+    for dt, K, d in combos:
+        cols = N if d == UP else M
+        if dt.kind == "f":
+            V = rng.standard_normal((K, cols)).astype(dt)
+        else:
+            V = rng.integers(0, 2, size=(K, cols)).astype(dt)
+        out.append(V)
+    return out
+
+
+def graph_stats(g):
+    info = g.info()
+    return {"nodes": info["num_nodes"], "edges": info["num_edges"], "samples": info["num_samples"],
+            "mutations": info["num_mutations"], "levels": info["num_levels"]}
+
+
+def alg_bytes(stats, K, s, direction):
+    """Algorithmic bytes of one traversal: edge ids once, node offsets, one operand row per edge,
+    each node accumulator written once, plus the seed/gather I/O."""
+    E, n, N, M = stats["edges"], stats["nodes"], stats["samples"], stats["mutations"]
+    cols_in, cols_out = (N, M) if direction == UP else (M, N)
+    return E * 4 + (n + 1) * 8 + E * K * s + n * K * s + K * (cols_in + cols_out) * s + 8 * M
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, device: int):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={device}", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        self.p.wait()
+        self.f.flush()
+        rows = [r.split(",") for r in Path(self.f.name).read_text().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm = [float(r[1]) for r in rows if len(r) >= 9 and r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if len(r) >= 9 and r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows if len(r) >= 9 for i in range(4) if "Active" in r[5 + i]
+                          and "Not" not in r[5 + i]})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def cpu_baseline(args, combos, seconds_budget, threads=None):
+    """The oracle port (the reference's range-split multi-core pattern) on a bounded sample of the
+    workload: the same generator with a prefix of the variants."""
+    import grgl_gb300 as gx
+    import oracle
+
+    oracle.build()
+    threads = threads or os.cpu_count() or 1
+    # size the sample: ~1.5e8 edge*K per core-second for the sharded restatement (probe below)
+    sample_m = max(1000, min(args.mutations, 20000))
+    g = gx.window_tree_grg(args.samples, sample_m, seed=args.seed)
+    a = g.export_arrays()
+    og = oracle.OracleGraph(num_samples=args.samples, ploidy=2, down_off=a["down_off"], down_adj=a["down_adj"],
+                            mut_node=a["mut_node"])
+    sh = oracle.Shards(og, threads)
+    rng = np.random.default_rng(1)
+    E = og.num_edges
+    total_units, total_t = 0, 0.0
+    t_start = time.perf_counter()
+    for dt, K, d in combos:
+        V = make_inputs(rng, [(dt, K, d)], og.num_samples, og.num_mutations)[0]
+        t0 = time.perf_counter()
+        sh.matmul(V, d)
+        total_t += time.perf_counter() - t0
+        total_units += E * K
+        if time.perf_counter() - t_start > seconds_budget:
+            break
+    return {"value": total_units / total_t, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"window-tree N={args.samples} M={sample_m} (E={E}); "
+                      f"{'all' if time.perf_counter() - t_start <= seconds_budget else 'first'} workload combos; "
+                      f"{total_units:.3g} edge*K in {total_t:.1f}s"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    combos = workload(args)
+    budget = max(5.0, args.cpu_seconds)
+    vals = []
+    cb = None
+    for _ in range(args.warmup + args.steps):
+        cb = cpu_baseline(args, combos, budget / max(1, args.steps))
+        vals.append(cb["value"])
+    v = statistics.median(vals[args.warmup:]) if len(vals) > args.warmup else vals[-1]
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "int32,float32,float64", "data": "synthetic (seeded window-tree GRG)", "impl": "reference",
+            "config": {"workload": f"plain matmul, window-tree GRG N={args.samples} M={args.mutations}, "
+                                   f"K in {{{args.ks}}}, UP+DOWN, {args.dtypes}"},
+            "cpu_baseline": dict(cb, value=v),
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import torch
+
+    import grgl_gb300 as gx
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    combos = workload(args)
+    t0 = time.perf_counter()
+    g = gx.window_tree_grg(args.samples, args.mutations, seed=args.seed + rank)
+    t_gen = time.perf_counter() - t0
+    stats = graph_stats(g)
+    t0 = time.perf_counter()
+    g.upload()
+    torch.cuda.synchronize()
+    t_up = time.perf_counter() - t0
+    stats["levels"] = g.info()["num_levels"]
+    stats["device_bytes"] = g.info()["device_bytes"]
+    rng = np.random.default_rng(7)
+    host_inputs = make_inputs(rng, combos, stats["samples"], stats["mutations"])
+    dev_inputs = [torch.from_numpy(V).cuda() for V in host_inputs]
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    def step(inputs, record):
+        for (dt, K, d), V in zip(combos, inputs):
+            gx.matmul(g, V, d)
+            if record is not None:
+                t = gx.last_timing()
+                record.append((dt, K, d, t))
+
+    # warm-up
+    for _ in range(args.warmup):
+        step(dev_inputs, None)
+    barrier()
+    gx.set_timing(True)
+    clocks = Clocks(local)
+    records = []
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    start.record()
+    for _ in range(args.steps):
+        step(dev_inputs, records)
+    end.record()
+    barrier()
+    clk = clocks.stop()
+    gx.set_timing(False)
+    ms = start.elapsed_time(end)
+    ms_t = torch.tensor([ms], device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(ms_t, op=torch.distributed.ReduceOp.MAX)
+    ms = float(ms_t.item())
+    units_per_step = sum(stats["edges"] * K for _, K, _ in combos)
+    value = units_per_step * args.steps * world / (ms / 1000.0)
+
+    # roofline of the sweep kernel over the timed region
+    sweep_ms = sum(t["sweep_ms"] for *_, t in records)
+    abytes = sum(alg_bytes(stats, K, dt.itemsize, d) for dt, K, d, _ in records)
+    compulsory = sum(stats["edges"] * 4 + (stats["nodes"] + 1) * 8 + 2 * stats["nodes"] * K * dt.itemsize
+                     for dt, K, d, _ in records)
+    launches = sum(t["launches"] for *_, t in records)
+    peaks = {}
+    pk = ROOT / "MEASURED_PEAKS.json"
+    if pk.exists():
+        peaks = json.loads(pk.read_text())
+    peak = peaks.get("hbm_gbs", 6800.0)
+    achieved = abytes / (sweep_ms / 1000.0) / 1e9
+    traffic = None
+    tfile = ROOT / "profiles" / "sweep_traffic.json"
+    if tfile.exists():
+        traffic = json.loads(tfile.read_text()).get("bytes_per_step")
+
+    # end to end: host buffers through the C-ABI (copies inside the timed region)
+    barrier()
+    h2d = sum(V.nbytes for V in host_inputs)
+    d2h = sum(K * (stats["mutations"] if d == UP else stats["samples"]) * dt.itemsize for dt, K, d in combos)
+    t0 = time.perf_counter()
+    e2e_steps = max(1, min(args.steps, 2))
+    for _ in range(e2e_steps):
+        step(host_inputs, None)
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    e2e_value = units_per_step * e2e_steps * world / e2e_s
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(args, combos, args.cpu_seconds)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int32,float32,float64", "data": "synthetic (seeded window-tree GRG)",
+            "config": {"workload": f"plain matmul, window-tree GRG N={args.samples} M={args.mutations} seed={args.seed}, "
+                                   f"K in {{{args.ks}}}, UP+DOWN, {args.dtypes}; 24 matmuls per step",
+                       "graph": stats, "l2": "inputs larger than L2 (edge CSR streamed every traversal)",
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "compulsory_frac": compulsory / (sweep_ms / 1000.0) / 1e9 / peak,
+                         "kernel": "grgx::sweep_kernel", "sweep_ms_per_step": sweep_ms / args.steps,
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback 6800"},
+            "clocks": clk,
+            "gpu_launches": launches,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "cpu_baseline": cpu,
+            "setup_s": {"generate": t_gen, "plan_upload": t_up},
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

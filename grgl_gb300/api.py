@@ -1,0 +1,339 @@
+"""Python mirror of pygrgl's matmul surface, running on the GB300 kernels of libgrgx.
+
+Names, argument meanings, output dtypes and error messages follow the reference binding
+(src/python/_grgl.cpp:80-241, :1141-1230): ``matmul(grg, input, direction, emit_all_nodes=False,
+by_individual=False, init=None, miss=None)`` returns a new K x cols array of the input's dtype;
+misuse raises ``RuntimeError`` with the reference's message text.
+
+Inputs may be numpy arrays (host memory; copies to and from the GPU are part of the call) or
+CUDA tensors (device memory; the call runs on the current torch stream and returns a CUDA
+tensor without synchronising).
+"""
+from __future__ import annotations
+
+import ctypes
+import enum
+import os
+import tempfile
+from typing import Optional
+
+import numpy as np
+
+from . import _lib
+
+INVALID_NODE = 0x7FFFFFFF  # include/grgl/grgnode.h:58
+COAL_COUNT_NOT_SET = 0xFFFFFFFF  # include/grgl/node_data.h:31
+
+
+class TraversalDirection(enum.IntEnum):
+    """include/grgl/visitor.h:26 (exported by _grgl.cpp:750-757)."""
+
+    DOWN = 1
+    UP = 2
+
+
+DOWN = TraversalDirection.DOWN
+UP = TraversalDirection.UP
+
+# numpy dtype -> grgx_dtype (include/grgx.h), in the order _grgl.cpp:205-238 dispatches.
+_DTYPE_CODES = {
+    np.dtype(np.float64): 0, np.dtype(np.float32): 1, np.dtype(np.int64): 2, np.dtype(np.int32): 3,
+    np.dtype(np.int16): 4, np.dtype(np.int8): 5, np.dtype(np.uint64): 6, np.dtype(np.uint32): 7,
+    np.dtype(np.uint16): 8, np.dtype(np.uint8): 9, np.dtype(np.bool_): 10,
+}
+_DOT_DTYPES = (np.dtype(np.float64), np.dtype(np.float32), np.dtype(np.int64), np.dtype(np.int32))
+
+
+def _check(cond: bool, msg: str):
+    if not cond:
+        raise RuntimeError(msg)
+
+
+class GRG:
+    """A GRG resident for matmul: host arrays plus, after first use, the device level plan.
+
+    Wraps a ``grgx_graph`` handle.  Immutable; safe to share between threads.
+    """
+
+    def __init__(self, handle: int):
+        self._h = ctypes.c_void_p(handle)
+        info = _lib.GraphInfo()
+        _lib.check(_lib.lib().grgx_graph_info_get(self._h, ctypes.byref(info)))
+        self._info = info
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                _lib.lib().grgx_graph_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    # -- properties named like pygrgl.GRG ----------------------------------------------------
+    @property
+    def num_nodes(self) -> int:
+        return int(self._info.num_nodes)
+
+    @property
+    def num_edges(self) -> int:
+        return int(self._info.num_edges)
+
+    @property
+    def num_samples(self) -> int:
+        return int(self._info.num_samples)
+
+    @property
+    def num_mutations(self) -> int:
+        return int(self._info.num_mutations)
+
+    @property
+    def ploidy(self) -> int:
+        return int(self._info.ploidy)
+
+    @property
+    def num_individuals(self) -> int:
+        return self.num_samples // self.ploidy
+
+    @property
+    def has_missing_data(self) -> bool:
+        return bool(self._info.has_missing)
+
+    @property
+    def has_coal_counts(self) -> bool:
+        return bool(self._info.has_coals)
+
+    def info(self) -> dict:
+        info = _lib.GraphInfo()
+        _lib.check(_lib.lib().grgx_graph_info_get(self._h, ctypes.byref(info)))
+        return {name: int(getattr(info, name)) for name, _ in info._fields_}
+
+    def upload(self) -> "GRG":
+        """Build the level plan and make it resident on the current CUDA device."""
+        _lib.check(_lib.lib().grgx_graph_upload(self._h))
+        return self
+
+    def export_arrays(self) -> dict:
+        """Copies of the down-edge CSR, mutation/missingness nodes and coal counts."""
+        n, e, m = self.num_nodes, self.num_edges, self.num_mutations
+        out = {
+            "down_off": np.zeros(n + 1, dtype=np.uint64),
+            "down_adj": np.zeros(e, dtype=np.uint32),
+            "mut_node": np.zeros(m, dtype=np.uint32),
+            "miss_node": np.zeros(m, dtype=np.uint32),
+            "coals": np.zeros(n - self.num_samples, dtype=np.uint32),
+        }
+        _lib.check(_lib.lib().grgx_graph_export(self._h, *(a.ctypes.data for a in out.values())))
+        return out
+
+    def get_down_edges(self, node: int) -> list:
+        a = self._cached_arrays()
+        return a["down_adj"][a["down_off"][node]:a["down_off"][node + 1]].tolist()
+
+    def get_sample_nodes(self) -> list:
+        return list(range(self.num_samples))
+
+    def _cached_arrays(self) -> dict:
+        if not hasattr(self, "_arrays"):
+            self._arrays = self.export_arrays()
+        return self._arrays
+
+    def __repr__(self) -> str:
+        return (f"<[grgl_gb300.GRG] mutations={self.num_mutations}, individuals={self.num_individuals}, "
+                f"ploidy={self.ploidy}, mutable=No>")
+
+
+def _new(fn, *args) -> GRG:
+    h = ctypes.c_void_p()
+    _lib.check(fn(*args, ctypes.byref(h)))
+    return GRG(h.value)
+
+
+def load_immutable_grg(filename: str, load_up_edges: bool = True) -> Optional[GRG]:
+    """pygrgl.load_immutable_grg (_grgl.cpp:937-953): None (and a message on stderr) on failure."""
+    h = ctypes.c_void_p()
+    status = _lib.lib().grgx_graph_load(os.fsencode(filename), ctypes.byref(h))
+    if status != _lib.OK:
+        import sys
+
+        print(f"Failed to load GRG: {_lib.last_error()}", file=sys.stderr)
+        return None
+    return GRG(h.value)
+
+
+def from_csr(num_samples: int, ploidy: int, down_off, down_adj, mut_node, miss_node=None, coals=None) -> GRG:
+    """A GRG from CSR arrays (children of node v: down_adj[down_off[v]:down_off[v+1]])."""
+    off = np.ascontiguousarray(down_off, dtype=np.uint64)
+    adj = np.ascontiguousarray(down_adj, dtype=np.uint32)
+    mut = np.ascontiguousarray(mut_node, dtype=np.uint32)
+    miss = None if miss_node is None else np.ascontiguousarray(miss_node, dtype=np.uint32)
+    co = None if coals is None else np.ascontiguousarray(coals, dtype=np.uint32)
+    return _new(_lib.lib().grgx_graph_from_csr, len(off) - 1, num_samples, ploidy, off.ctypes.data,
+                adj.ctypes.data if len(adj) else None, len(mut), mut.ctypes.data if len(mut) else None,
+                miss.ctypes.data if miss is not None else None, co.ctypes.data if co is not None else None)
+
+
+def from_pygrgl(grg) -> GRG:
+    """Convert a reference ``pygrgl.GRG`` (saved unsimplified through pygrgl.save_grg, then loaded)."""
+    import pygrgl  # the caller's reference installation
+
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "g.grg")
+        pygrgl.save_grg(grg, path, False)
+        out = load_immutable_grg(path)
+    _check(out is not None, "conversion from pygrgl failed")
+    return out
+
+
+def window_tree_grg(num_samples: int, num_mutations: int, seed: int = 42, window: int = 100,
+                    threads: int = 0) -> GRG:
+    """Seeded window-tree GRG (one Kingman tree per window, collapsed to mutation nodes)."""
+    return _new(_lib.lib().grgx_graph_generate, num_samples, num_mutations, seed, window, threads)
+
+
+def _is_torch_cuda(x) -> bool:
+    mod = type(x).__module__
+    return mod.startswith("torch") and getattr(x, "is_cuda", False)
+
+
+def _torch_dtype_to_np(t):
+    import torch
+
+    return {torch.float64: np.float64, torch.float32: np.float32, torch.int64: np.int64, torch.int32: np.int32,
+            torch.int16: np.int16, torch.int8: np.int8, torch.uint8: np.uint8, torch.bool: np.bool_}.get(t)
+
+
+def matmul(grg: GRG, input, direction, emit_all_nodes: bool = False, by_individual: bool = False, init=None,
+           miss=None, *, f32_compensated: bool = True):
+    """pygrgl.matmul on the GPU (reference: _grgl.cpp:187-241, grg.h:1341-1517).
+
+    ``f32_compensated`` (float32 only, default True) accumulates with TwoSum compensation; False
+    gives plain float summation.
+    """
+    if _is_torch_cuda(input):
+        return _matmul_device(grg, input, direction, emit_all_nodes, by_individual, init, miss, f32_compensated)
+    direction = TraversalDirection(int(direction))
+    if not isinstance(input, np.ndarray):
+        raise RuntimeError(f"Unsupported numpy dtype: {np.asarray(input).dtype}")
+    arr = np.ascontiguousarray(input)
+    _check(arr.ndim == 2, "matmul() only support two dimensional numpy arrays as input.")
+    rows, cols = arr.shape
+    _check(rows != 0 and cols != 0, "matmul() requires non-zero dimensions.")
+    _check(arr.dtype in _DTYPE_CODES, f"Unsupported numpy dtype: {arr.dtype}")
+    code = _DTYPE_CODES[arr.dtype]
+    nsamp = grg.num_individuals if by_individual else grg.num_samples
+    out_cols = grg.num_nodes if emit_all_nodes else (nsamp if direction == DOWN else grg.num_mutations)
+    init_kind, init_arr = _parse_init(grg, init, arr.dtype, rows, code == 10)
+    miss_arr = _parse_miss(miss, arr.dtype, rows, cols, out_cols, direction, emit_all_nodes)
+    out = np.empty((rows, out_cols), dtype=arr.dtype)
+    flags = _lib.FLAG_OVERWRITE | (0 if f32_compensated else _lib.FLAG_F32_PLAIN)
+    _lib.check(_lib.lib().grgx_matmul(grg._h, code, arr.ctypes.data, cols, rows, int(direction), out.ctypes.data,
+                                      out.size, int(bool(emit_all_nodes)), int(bool(by_individual)),
+                                      init_arr.ctypes.data if init_arr is not None else None, init_kind,
+                                      miss_arr.ctypes.data if miss_arr is not None else None, flags, None))
+    if miss_arr is not None and miss_arr is not miss:
+        miss[...] = miss_arr
+    return out
+
+
+def _parse_init(grg, init, dtype, rows, is_bool):
+    """init handling of dispatchMult (_grgl.cpp:116-142)."""
+    if init is None:
+        return 0, None
+    _check(not is_bool, "init=... is not supported with boolean dtype")
+    if isinstance(init, str):
+        _check(init == "xtx", f"Unexpected init value: {init}")
+        return 3, None
+    arr = init if _is_torch_cuda(init) else np.asarray(init)
+    got = _torch_dtype_to_np(arr.dtype) if _is_torch_cuda(arr) else arr.dtype
+    _check(isinstance(init, np.ndarray) or _is_torch_cuda(init), f"The init matrix must match the dtype of the "
+           f"input matrix. Got: {np.asarray(init).dtype}")
+    _check(np.dtype(got) == dtype, f"The init matrix must match the dtype of the input matrix. Got: {np.dtype(got)}")
+    if arr.ndim == 1:
+        _check(arr.shape[0] == rows,
+               "If init has a single dimension, it must match the number of rows in the input matrix")
+        return 1, (arr.contiguous() if _is_torch_cuda(arr) else np.ascontiguousarray(arr))
+    if arr.ndim == 2:
+        _check(tuple(arr.shape) == (rows, grg.num_nodes),
+               "If init is a matrix, it must match the dimensions ROW x NODES")
+        return 2, (arr.contiguous() if _is_torch_cuda(arr) else np.ascontiguousarray(arr))
+    return 0, None
+
+
+def _parse_miss(miss, dtype, rows, cols, out_cols, direction, emit_all):
+    """miss handling of dispatchMult (_grgl.cpp:144-167)."""
+    if miss is None:
+        return None
+    _check(not emit_all, 'The "miss" parameter cannot be mixed with the "emit_all_nodes" parameter')
+    if _is_torch_cuda(miss):
+        got = np.dtype(_torch_dtype_to_np(miss.dtype))
+    else:
+        _check(isinstance(miss, np.ndarray),
+               f'The "miss" input must be a matrix with dtype matching the input matrix. Got: '
+               f'{np.asarray(miss).dtype}')
+        got = miss.dtype
+    _check(got == dtype, f'The "miss" input must be a matrix with dtype matching the input matrix. Got: {got}')
+    _check(miss.ndim == 2, f'"miss" must be a two-dimension numpy array (matrix). ndim={miss.ndim}')
+    mrows, mcols = miss.shape
+    _check(mrows == rows, f'"miss" has {mrows} rows, but must match the input and output matrices ({rows})')
+    if direction == DOWN:
+        _check(mcols == cols, f'The "miss" matrix must match the number of columns in the input matrix. Got: {mcols}')
+    else:
+        _check(mcols == out_cols,
+               f'The "miss" matrix must match the number of columns in the output matrix. Got: {mcols}')
+    if _is_torch_cuda(miss):
+        _check(miss.is_contiguous(), '"miss" must be contiguous')
+        return miss
+    return miss if miss.flags.c_contiguous else np.ascontiguousarray(miss)
+
+
+def _matmul_device(grg, x, direction, emit_all, by_indiv, init, miss, f32_compensated):
+    import torch
+
+    direction = TraversalDirection(int(direction))
+    _check(x.dim() == 2, "matmul() only support two dimensional numpy arrays as input.")
+    x = x.contiguous()
+    rows, cols = x.shape
+    _check(rows != 0 and cols != 0, "matmul() requires non-zero dimensions.")
+    npd = _torch_dtype_to_np(x.dtype)
+    _check(npd is not None, f"Unsupported dtype: {x.dtype}")
+    code = _DTYPE_CODES[np.dtype(npd)]
+    nsamp = grg.num_individuals if by_indiv else grg.num_samples
+    out_cols = grg.num_nodes if emit_all else (nsamp if direction == DOWN else grg.num_mutations)
+    init_kind, init_t = _parse_init(grg, init, np.dtype(npd), rows, code == 10)
+    if init_t is not None and not _is_torch_cuda(init_t):
+        init_t = torch.from_numpy(np.ascontiguousarray(init_t)).to(x.device)
+    miss_t = _parse_miss(miss, np.dtype(npd), rows, cols, out_cols, direction, emit_all)
+    _check(miss_t is None or _is_torch_cuda(miss_t), '"miss" must be a CUDA tensor when the input is one')
+    out = torch.empty((rows, out_cols), dtype=x.dtype, device=x.device)
+    stream = torch.cuda.current_stream(x.device).cuda_stream
+    flags = _lib.FLAG_OVERWRITE | _lib.FLAG_DEVICE_POINTERS | (0 if f32_compensated else _lib.FLAG_F32_PLAIN)
+    with torch.cuda.device(x.device):
+        _lib.check(_lib.lib().grgx_matmul(grg._h, code, x.data_ptr(), cols, rows, int(direction), out.data_ptr(),
+                                          out.numel(), int(bool(emit_all)), int(bool(by_indiv)),
+                                          init_t.data_ptr() if init_t is not None else None, init_kind,
+                                          miss_t.data_ptr() if miss_t is not None else None, flags, stream))
+    return out
+
+
+def dot_product(grg: GRG, input, direction):
+    """pygrgl.dot_product (_grgl.cpp:80-98): 1-D input, f64/f32/i64/i32 only."""
+    if not isinstance(input, np.ndarray):
+        raise RuntimeError(f"Unsupported numpy dtype: {np.asarray(input).dtype}")
+    arr = np.ascontiguousarray(input)
+    _check(arr.ndim == 1, "dot_product() only support one-dimensional numpy arrays as input.")
+    _check(arr.shape[0] != 0, "dot_product() requires non-empty array input.")
+    _check(arr.dtype in _DOT_DTYPES, f"Unsupported numpy dtype: {arr.dtype}")
+    return matmul(grg, arr.reshape(1, -1), direction)[0]
+
+
+def set_timing(enabled: bool):
+    """Per-call CUDA-event timing on this thread (see last_timing)."""
+    _lib.lib().grgx_set_timing(int(bool(enabled)))
+
+
+def last_timing() -> dict:
+    t = _lib.Timing()
+    _lib.check(_lib.lib().grgx_last_timing(ctypes.byref(t)))
+    return {"total_ms": t.total_ms, "sweep_ms": t.sweep_ms, "launches": int(t.launches),
+            "alg_bytes": int(t.alg_bytes)}

@@ -1,0 +1,207 @@
+// The C ABI (include/grgx.h): exception-free wrappers over the host graph, the plan and the
+// matmul orchestration.
+#include <cstring>
+#include <string>
+
+#include "grgx_internal.h"
+
+namespace grgx {
+DevicePlan* ensure_device_plan(grgx_graph* g);
+uint64_t device_plan_bytes(const grgx_graph* g);
+uint64_t device_plan_levels(const grgx_graph* g);
+void matmul_impl(grgx_graph* g, int dtype, const void* input, uint64_t in_cols, uint64_t rows, int direction,
+                 void* output, uint64_t output_size, int emit_all, int by_indiv, const void* init, int init_kind,
+                 void* miss, uint32_t flags, void* stream);
+void set_timing(int enabled);
+grgx_timing last_timing();
+
+namespace {
+thread_local std::string t_error;
+
+template <typename F> grgx_status guarded(F&& f) {
+    try {
+        f();
+        t_error.clear();
+        return GRGX_OK;
+    } catch (const Error& e) {
+        t_error = e.what();
+        return static_cast<grgx_status>(e.code);
+    } catch (const std::bad_alloc&) {
+        t_error = "host out of memory";
+        return GRGX_ERR_OUT_OF_MEMORY;
+    } catch (const std::exception& e) {
+        t_error = e.what();
+        return GRGX_ERR_CUDA;
+    }
+}
+
+uint64_t count_levels(const HostGraph& g) {
+    // Heights without building the plan (ordered graphs: one pass).
+    std::vector<uint32_t> h(g.num_nodes, 0);
+    uint32_t mx = 0;
+    for (uint64_t v = 0; v < g.num_nodes; v++) {
+        uint32_t x = 0;
+        for (uint64_t e = g.down_off[v]; e < g.down_off[v + 1]; e++) {
+            const uint32_t c = g.down_adj[e];
+            if (c >= v) return 0;  // not ordered: unknown until the plan is built
+            x = std::max(x, h[c] + 1);
+        }
+        h[v] = x;
+        mx = std::max(mx, x);
+    }
+    return g.num_nodes ? mx + 1 : 0;
+}
+}  // namespace
+
+void set_last_error(const std::string& msg) { t_error = msg; }
+
+}  // namespace grgx
+
+using namespace grgx;
+
+extern "C" {
+
+const char* grgx_last_error(void) { return t_error.c_str(); }
+
+const char* grgx_version(void) { return "grgx 0.1 (sm_103a)"; }
+
+grgx_status grgx_graph_load(const char* path, grgx_graph** out) {
+    return guarded([&] {
+        GRGX_CHECK(path && out, GRGX_ERR_API_MISUSE, "null argument");
+        auto g = new grgx_graph();
+        try {
+            g->host = load_grg_file(path);
+        } catch (...) {
+            delete g;
+            throw;
+        }
+        *out = g;
+    });
+}
+
+grgx_status grgx_graph_from_csr(uint64_t num_nodes, uint64_t num_samples, uint64_t ploidy, const uint64_t* down_off,
+                                const uint32_t* down_adj, uint64_t num_mutations, const uint32_t* mut_node,
+                                const uint32_t* miss_node, const uint32_t* coals, grgx_graph** out) {
+    return guarded([&] {
+        GRGX_CHECK(out && down_off && (num_mutations == 0 || mut_node), GRGX_ERR_API_MISUSE, "null argument");
+        GRGX_CHECK(num_nodes <= MAX_NODES && num_samples <= num_nodes, GRGX_ERR_API_MISUSE, "invalid node counts");
+        GRGX_CHECK(ploidy > 0, GRGX_ERR_API_MISUSE, "ploidy must be positive");
+        auto h = std::make_unique<HostGraph>();
+        h->num_nodes = num_nodes;
+        h->num_samples = num_samples;
+        h->ploidy = ploidy;
+        h->num_mutations = num_mutations;
+        h->down_off.assign(down_off, down_off + num_nodes + 1);
+        GRGX_CHECK(h->down_off[0] == 0, GRGX_ERR_API_MISUSE, "down_off[0] must be 0");
+        for (uint64_t v = 0; v < num_nodes; v++)
+            GRGX_CHECK(h->down_off[v + 1] >= h->down_off[v], GRGX_ERR_API_MISUSE, "down_off must be nondecreasing");
+        const uint64_t E = h->down_off[num_nodes];
+        GRGX_CHECK(E == 0 || down_adj, GRGX_ERR_API_MISUSE, "null argument");
+        h->down_adj.assign(down_adj, down_adj + E);
+        for (uint32_t c : h->down_adj) GRGX_CHECK(c < num_nodes, GRGX_ERR_API_MISUSE, "edge target out of range");
+        h->mut_node.assign(mut_node, mut_node + num_mutations);
+        for (uint32_t m : h->mut_node)
+            GRGX_CHECK(m == INVALID_NODE || m < num_nodes, GRGX_ERR_API_MISUSE, "mutation node out of range");
+        if (miss_node) {
+            h->miss_node.assign(miss_node, miss_node + num_mutations);
+            for (uint32_t m : h->miss_node)
+                GRGX_CHECK(m == INVALID_NODE || m < num_nodes, GRGX_ERR_API_MISUSE, "missingness node out of range");
+        }
+        if (coals) h->coals.assign(coals, coals + (num_nodes - num_samples));
+        auto g = new grgx_graph();
+        g->host = std::move(h);
+        *out = g;
+    });
+}
+
+grgx_status grgx_graph_generate(uint64_t num_samples, uint64_t num_mutations, uint64_t seed, uint32_t window,
+                                int threads, grgx_graph** out) {
+    return guarded([&] {
+        GRGX_CHECK(out && num_samples >= 2 && window >= 1, GRGX_ERR_API_MISUSE, "invalid generator arguments");
+        auto g = new grgx_graph();
+        try {
+            g->host = generate_window_tree(num_samples, num_mutations, seed, window, threads);
+        } catch (...) {
+            delete g;
+            throw;
+        }
+        *out = g;
+    });
+}
+
+void grgx_graph_destroy(grgx_graph* g) {
+    if (!g) return;
+    try {
+        delete g;
+    } catch (...) {
+    }
+}
+
+grgx_status grgx_graph_info_get(const grgx_graph* g, grgx_graph_info* out) {
+    return guarded([&] {
+        GRGX_CHECK(g && out, GRGX_ERR_API_MISUSE, "null argument");
+        const HostGraph& h = *g->host;
+        std::memset(out, 0, sizeof(*out));
+        out->num_nodes = h.num_nodes;
+        out->num_edges = h.num_edges();
+        out->num_samples = h.num_samples;
+        out->num_mutations = h.num_mutations;
+        out->ploidy = h.ploidy;
+        out->num_levels = g->dev ? device_plan_levels(g) : count_levels(h);
+        out->has_missing = h.miss_node.empty() ? 0 : 1;
+        bool coals = h.coals.size() >= h.num_nodes - h.num_samples;
+        for (uint64_t i = 0; coals && i < h.num_nodes - h.num_samples; i++) coals = (h.coals[i] != COAL_NOT_SET);
+        out->has_coals = coals ? 1 : 0;
+        out->device_bytes = device_plan_bytes(g);
+    });
+}
+
+grgx_status grgx_graph_export(const grgx_graph* g, uint64_t* down_off, uint32_t* down_adj, uint32_t* mut_node,
+                              uint32_t* miss_node, uint32_t* coals) {
+    return guarded([&] {
+        GRGX_CHECK(g, GRGX_ERR_API_MISUSE, "null argument");
+        const HostGraph& h = *g->host;
+        if (down_off) std::memcpy(down_off, h.down_off.data(), h.down_off.size() * sizeof(uint64_t));
+        if (down_adj && !h.down_adj.empty())
+            std::memcpy(down_adj, h.down_adj.data(), h.down_adj.size() * sizeof(uint32_t));
+        if (mut_node && !h.mut_node.empty())
+            std::memcpy(mut_node, h.mut_node.data(), h.mut_node.size() * sizeof(uint32_t));
+        if (miss_node) {
+            for (uint64_t m = 0; m < h.num_mutations; m++)
+                miss_node[m] = h.miss_node.empty() ? INVALID_NODE : h.miss_node[m];
+        }
+        if (coals) {
+            for (uint64_t i = 0; i < h.num_nodes - h.num_samples; i++)
+                coals[i] = (i < h.coals.size()) ? h.coals[i] : COAL_NOT_SET;
+        }
+    });
+}
+
+grgx_status grgx_graph_upload(grgx_graph* g) {
+    return guarded([&] {
+        GRGX_CHECK(g, GRGX_ERR_API_MISUSE, "null argument");
+        ensure_device_plan(g);
+    });
+}
+
+grgx_status grgx_matmul(grgx_graph* g, grgx_dtype dtype, const void* input, uint64_t input_cols, uint64_t input_rows,
+                        grgx_direction direction, void* output, uint64_t output_size, int emit_all_nodes,
+                        int by_individual, const void* init, grgx_init init_kind, void* miss, uint32_t flags,
+                        void* stream) {
+    return guarded([&] {
+        GRGX_CHECK(g && input && output, GRGX_ERR_API_MISUSE, "null argument");
+        matmul_impl(g, dtype, input, input_cols, input_rows, direction, output, output_size, emit_all_nodes,
+                    by_individual, init, init_kind, miss, flags, stream);
+    });
+}
+
+void grgx_set_timing(int enabled) { set_timing(enabled); }
+
+grgx_status grgx_last_timing(grgx_timing* out) {
+    return guarded([&] {
+        GRGX_CHECK(out, GRGX_ERR_API_MISUSE, "null argument");
+        *out = last_timing();
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,41 @@
+// Host-side launch entry points of the device kernels (internal to libgrgx).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "sweep.cuh"
+
+namespace grgx {
+
+// Storage/accumulation kinds (see ops.cuh).
+enum class Kind { U32, U64, F64, F32C, F32, XOR };
+
+// One level (or seed pass) of the sweep; VW elements per lane, G lanes per row.
+void launch_sweep_u32(const SweepParams<uint32_t>& p, int vw, int g, dim3 grid, cudaStream_t s);
+void launch_sweep_xor(const SweepParams<uint32_t>& p, int vw, int g, dim3 grid, cudaStream_t s);
+void launch_sweep_u64(const SweepParams<unsigned long long>& p, int vw, int g, dim3 grid, cudaStream_t s);
+void launch_sweep_f64(const SweepParams<double>& p, int vw, int g, dim3 grid, cudaStream_t s);
+void launch_sweep_f32c(const SweepParams<float>& p, int vw, int g, dim3 grid, cudaStream_t s);
+void launch_sweep_f32(const SweepParams<float>& p, int vw, int g, dim3 grid, cudaStream_t s);
+
+// Column-map modes of the transposing loads/stores.
+enum MapMode { MAP_IDENT = 0, MAP_DIV = 1, MAP_TABLE = 2, MAP_FOLD = 3 };
+
+// dst[i*stride + k] (=, or += when add) IO->S(src[k*ld + col(i)]) for i < R, k < K; columns
+// K..stride-1 are zeroed when assigning.  col(i) = i, i/div, or tab[i].
+void launch_load_rows(int dtype, const void* src, long long K, long long ld, long long R, int mode, long long div,
+                      const uint32_t* tab, void* dst, long long stride, int add, cudaStream_t s);
+
+// out[k*ld + c] (=, or += when add) S->IO(vals[map(c)]) for c < C, k < K; map(c) = c, tab[c]
+// (INVALID -> 0), or the sum of rows c*fold .. c*fold+fold-1.
+void launch_store_cols(int dtype, const void* vals, long long stride, long long K, long long C, int mode,
+                       long long fold, const uint32_t* tab, void* out, long long ld, int add, cudaStream_t s);
+
+// Node-value initialisation: VECTOR (vals[v][k] = init[k]) and XTX (vals[v][k] = xtx[v]).
+void launch_init_vector(int dtype, const void* init, long long K, long long n, void* vals, long long stride,
+                        cudaStream_t s);
+void launch_init_xtx(int dtype, const uint32_t* xtx, long long K, long long n, void* vals, long long stride,
+                     cudaStream_t s);
+
+}  // namespace grgx

@@ -1,0 +1,470 @@
+// Device plan upload and the matmul orchestration behind grgx_matmul.
+//
+// One call is, on one stream:
+//   init      memset / VECTOR / MATRIX / XTX fill of the node values   (grg.h:1370-1402)
+//   seed      UP: samples <- input columns (transposing load)          (grg.h:1458-1469)
+//             DOWN: input -> per-mutation rows, then one gather-sum pass over the
+//             node -> mutations CSR (and the missingness CSR)          (grg.h:1405-1427)
+//   sweep     one launch per level, pull form, no atomics on values   (grg.h:1428-1431, 1470-1474)
+//   gather    node rows -> output columns (transposing store)          (grg.h:1440-1453, 1483-1516)
+// Scratch (node values, transposed inputs, heavy-row partials) comes from the device's
+// stream-ordered memory pool and is released on the same stream.
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <sstream>
+#include <thread>
+
+#include "grgx_internal.h"
+#include "launch.h"
+
+namespace grgx {
+
+#define GRGX_CUDA(call)                                                                               \
+    do {                                                                                             \
+        cudaError_t err__ = (call);                                                                  \
+        if (err__ != cudaSuccess) {                                                                  \
+            const int code__ = (err__ == cudaErrorMemoryAllocation) ? GRGX_ERR_OUT_OF_MEMORY         \
+                                                                    : GRGX_ERR_CUDA;                 \
+            throw ::grgx::Error(code__, std::string(#call) + ": " + cudaGetErrorString(err__));       \
+        }                                                                                            \
+    } while (0)
+
+struct DevCSR {
+    uint32_t* adj = nullptr;
+    int* rows = nullptr;
+    ChunkDev* chunks = nullptr;
+    HeavyDev* heavy = nullptr;
+    std::vector<int32_t> lb, le;
+    long long n_heavy = 0, n_pieces = 0, n_edges = 0, n_rows = 0;
+};
+
+struct DevicePlan {
+    int device = -1;
+    DevCSR up, down, seed, miss;
+    uint32_t* mut_new = nullptr;
+    uint32_t* miss_new = nullptr;
+    uint32_t* old2new = nullptr;
+    uint32_t* new2old = nullptr;
+    uint32_t* xtx_new = nullptr;
+    uint64_t bytes = 0;
+    uint64_t num_levels = 0;
+    bool has_coals = false;
+    bool has_miss = false;
+    std::vector<void*> allocs;
+};
+
+void destroy_device_plan(DevicePlan* p) {
+    if (!p) return;
+    int cur = -1;
+    cudaGetDevice(&cur);
+    cudaSetDevice(p->device);
+    for (void* a : p->allocs) cudaFree(a);
+    if (cur >= 0) cudaSetDevice(cur);
+    delete p;
+}
+
+namespace {
+
+static_assert(sizeof(Chunk) == sizeof(ChunkDev), "chunk layout");
+static_assert(sizeof(HeavyRow) == sizeof(HeavyDev), "heavy layout");
+
+template <typename T> T* upload(DevicePlan& d, const std::vector<T>& v) {
+    if (v.empty()) return nullptr;
+    void* p = nullptr;
+    GRGX_CUDA(cudaMalloc(&p, v.size() * sizeof(T)));
+    d.allocs.push_back(p);
+    d.bytes += v.size() * sizeof(T);
+    GRGX_CUDA(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return static_cast<T*>(p);
+}
+
+DevCSR upload_csr(DevicePlan& d, const PullCSR& c) {
+    DevCSR r;
+    r.adj = upload(d, c.adj);
+    r.rows = upload(d, c.rows);
+    r.chunks = reinterpret_cast<ChunkDev*>(upload(d, c.chunks));
+    r.heavy = reinterpret_cast<HeavyDev*>(upload(d, c.heavy));
+    r.lb = c.level_chunk_begin;
+    r.le = c.level_chunk_end;
+    r.n_heavy = static_cast<long long>(c.heavy.size());
+    r.n_pieces = c.num_pieces;
+    r.n_edges = static_cast<long long>(c.adj.size());
+    r.n_rows = static_cast<long long>(c.rows.size());
+    return r;
+}
+
+void setup_pool_once(int device) {
+    static std::mutex mu;
+    static std::vector<int> done;
+    std::lock_guard<std::mutex> lk(mu);
+    for (int d : done)
+        if (d == device) return;
+    cudaMemPool_t pool;
+    GRGX_CUDA(cudaDeviceGetDefaultMemPool(&pool, device));
+    uint64_t threshold = UINT64_MAX;
+    GRGX_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &threshold));
+    done.push_back(device);
+}
+
+struct Layout {
+    Kind kind;
+    int ssize;     // storage bytes per element
+    int asize;     // accumulator bytes per element (heavy partials)
+    long long stride;
+    int vw, g, ntiles;
+};
+
+long long next_pow2(long long x) {
+    long long p = 1;
+    while (p < x) p <<= 1;
+    return p;
+}
+
+Layout choose_layout(int dtype, long long K, bool plainF32) {
+    Layout L{};
+    long long base = K;
+    switch (dtype) {
+    case GRGX_F64: L.kind = Kind::F64; L.ssize = 8; break;
+    case GRGX_F32: L.kind = plainF32 ? Kind::F32 : Kind::F32C; L.ssize = 4; break;
+    case GRGX_I64: case GRGX_U64: L.kind = Kind::U64; L.ssize = 8; break;
+    case GRGX_BOOL: L.kind = Kind::XOR; L.ssize = 4; base = (K + 31) / 32; break;
+    default: L.kind = Kind::U32; L.ssize = 4; break;
+    }
+    L.asize = (L.kind == Kind::F32C) ? 8 : L.ssize;
+    const int maxVw = 16 / L.ssize;
+    if (base == 1) {
+        L.stride = 1; L.vw = 1; L.g = 1; L.ntiles = 1;
+    } else if (base == 2 && maxVw == 4) {
+        L.stride = 2; L.vw = 2; L.g = 1; L.ntiles = 1;
+    } else {
+        L.vw = maxVw;
+        L.stride = (base + maxVw - 1) / maxVw * maxVw;
+        const long long vecs = L.stride / L.vw;
+        L.g = static_cast<int>(std::min<long long>(32, next_pow2(vecs)));
+        L.ntiles = static_cast<int>((vecs + L.g - 1) / L.g);
+    }
+    return L;
+}
+
+struct Scratch {
+    cudaStream_t s;
+    std::vector<void*> ptrs;
+    explicit Scratch(cudaStream_t st) : s(st) {}
+    void* get(size_t bytes) {
+        if (bytes == 0) bytes = 16;
+        void* p = nullptr;
+        GRGX_CUDA(cudaMallocAsync(&p, bytes, s));
+        ptrs.push_back(p);
+        return p;
+    }
+    ~Scratch() {
+        for (void* p : ptrs) cudaFreeAsync(p, s);
+    }
+};
+
+thread_local bool t_timing = false;
+thread_local grgx_timing t_last{};
+
+template <typename S>
+SweepParams<S> make_params(const DevCSR& c, long long cb, long long ce, const void* src, void* dst, long long stride,
+                           int rmw, void* partials, unsigned* tickets, int ntiles) {
+    SweepParams<S> p;
+    p.adj = c.adj;
+    p.rows = c.rows;
+    p.chunks = c.chunks;
+    p.heavy = c.heavy;
+    p.c_begin = cb;
+    p.c_end = ce;
+    p.src = static_cast<const S*>(src);
+    p.dst = static_cast<S*>(dst);
+    p.stride = stride;
+    p.rmw = rmw;
+    p.partials = partials;
+    p.tickets = tickets;
+    p.ntiles = ntiles;
+    return p;
+}
+
+// Launches one level of a CSR; returns the number of kernels launched (0 or 1).
+int launch_level(const Layout& L, const DevCSR& c, size_t level, const void* src, void* dst, int rmw,
+                 void* partials, unsigned* tickets, cudaStream_t s) {
+    const long long cb = c.lb[level], ce = c.le[level];
+    if (ce <= cb) return 0;
+    const dim3 grid(static_cast<unsigned>((ce - cb + 7) / 8), static_cast<unsigned>(L.ntiles));
+    switch (L.kind) {
+    case Kind::U32:
+        launch_sweep_u32(make_params<uint32_t>(c, cb, ce, src, dst, L.stride, rmw, partials, tickets, L.ntiles),
+                         L.vw, L.g, grid, s);
+        break;
+    case Kind::XOR:
+        launch_sweep_xor(make_params<uint32_t>(c, cb, ce, src, dst, L.stride, rmw, partials, tickets, L.ntiles),
+                         L.vw, L.g, grid, s);
+        break;
+    case Kind::U64:
+        launch_sweep_u64(
+            make_params<unsigned long long>(c, cb, ce, src, dst, L.stride, rmw, partials, tickets, L.ntiles), L.vw,
+            L.g, grid, s);
+        break;
+    case Kind::F64:
+        launch_sweep_f64(make_params<double>(c, cb, ce, src, dst, L.stride, rmw, partials, tickets, L.ntiles),
+                         L.vw, L.g, grid, s);
+        break;
+    case Kind::F32C:
+        launch_sweep_f32c(make_params<float>(c, cb, ce, src, dst, L.stride, rmw, partials, tickets, L.ntiles),
+                          L.vw, L.g, grid, s);
+        break;
+    case Kind::F32:
+        launch_sweep_f32(make_params<float>(c, cb, ce, src, dst, L.stride, rmw, partials, tickets, L.ntiles),
+                         L.vw, L.g, grid, s);
+        break;
+    }
+    return 1;
+}
+
+size_t io_size(int dtype) {
+    switch (dtype) {
+    case GRGX_F64: case GRGX_I64: case GRGX_U64: return 8;
+    case GRGX_F32: case GRGX_I32: case GRGX_U32: return 4;
+    case GRGX_I16: case GRGX_U16: return 2;
+    default: return 1;
+    }
+}
+
+}  // namespace
+
+DevicePlan* ensure_device_plan(grgx_graph* g) {
+    std::lock_guard<std::mutex> lk(g->mu);
+    int device = 0;
+    GRGX_CUDA(cudaGetDevice(&device));
+    if (g->dev) {
+        GRGX_CHECK(g->dev->device == device, GRGX_ERR_UNSUPPORTED,
+                   "graph is resident on device " + std::to_string(g->dev->device));
+        return g->dev.get();
+    }
+    setup_pool_once(device);
+    if (!g->plan) g->plan = build_plan(*g->host);
+    const HostPlan& hp = *g->plan;
+    std::unique_ptr<DevicePlan, DevicePlanDeleter> d(new DevicePlan());
+    d->device = device;
+    d->up = upload_csr(*d, hp.up);
+    d->down = upload_csr(*d, hp.down);
+    d->seed = upload_csr(*d, hp.seed);
+    d->miss = upload_csr(*d, hp.miss);
+    d->mut_new = upload(*d, hp.mut_new);
+    d->miss_new = upload(*d, hp.miss_new);
+    d->old2new = upload(*d, hp.old2new);
+    d->new2old = upload(*d, hp.new2old);
+    d->xtx_new = upload(*d, hp.xtx_new);
+    d->num_levels = hp.num_levels;
+    d->has_coals = hp.has_coals;
+    d->has_miss = hp.has_miss;
+    g->dev = std::move(d);
+    g->plan.reset();  // the device copy is authoritative; free the host copy
+    return g->dev.get();
+}
+
+uint64_t device_plan_bytes(const grgx_graph* g) { return g->dev ? g->dev->bytes : 0; }
+uint64_t device_plan_levels(const grgx_graph* g) { return g->dev ? g->dev->num_levels : 0; }
+
+void matmul_impl(grgx_graph* g, int dtype, const void* input, uint64_t in_cols, uint64_t rows, int direction,
+                 void* output, uint64_t output_size, int emit_all, int by_indiv, const void* init, int init_kind,
+                 void* miss, uint32_t flags, void* stream_ptr) {
+    const HostGraph& hg = *g->host;
+    const uint64_t n = hg.num_nodes, N = hg.num_samples, M = hg.num_mutations, P = hg.ploidy;
+    // ---- validation: validateMatMulInputs (internal_mult.h:130-158) and the binding ----------
+    GRGX_CHECK(dtype >= GRGX_F64 && dtype <= GRGX_BOOL, GRGX_ERR_API_MISUSE, "Unsupported dtype");
+    GRGX_CHECK(direction == GRGX_DIRECTION_DOWN || direction == GRGX_DIRECTION_UP, GRGX_ERR_API_MISUSE,
+               "Invalid traversal direction");
+    GRGX_CHECK(in_cols > 0 && rows > 0, GRGX_ERR_API_MISUSE, "matmul() requires non-zero dimensions.");
+    GRGX_CHECK(output_size % rows == 0, GRGX_ERR_API_MISUSE, "Output size must be divisible by the number of rows");
+    const uint64_t out_cols = output_size / rows;
+    GRGX_CHECK(!by_indiv || N % P == 0, GRGX_ERR_API_MISUSE,
+               "by_individual needs the number of samples to be a multiple of the ploidy");
+    GRGX_CHECK(rows <= (dtype == GRGX_BOOL ? 65535ull : 2000000ull), GRGX_ERR_UNSUPPORTED,
+               "too many input rows for one call; split the rows");
+    const uint64_t expectSampleCols = by_indiv ? N / P : N;
+    if (direction == GRGX_DIRECTION_DOWN) {
+        GRGX_CHECK(in_cols == M, GRGX_ERR_API_MISUSE, "Input vector is not size M (numMutations)");
+        GRGX_CHECK(emit_all || out_cols == expectSampleCols, GRGX_ERR_API_MISUSE,
+                   "Output vector is not size N (numSamples, or numIndividuals depending on flags)");
+    } else {
+        GRGX_CHECK(in_cols == expectSampleCols, GRGX_ERR_API_MISUSE,
+                   "Input vector is not size N (numSamples, or numIndividuals depending on flags)");
+        GRGX_CHECK(emit_all || out_cols == M, GRGX_ERR_API_MISUSE, "Output vector is not size M (numMutations)");
+    }
+    GRGX_CHECK(!emit_all || out_cols == n, GRGX_ERR_API_MISUSE, "Output vector is not size numNodes");
+    GRGX_CHECK(init_kind == GRGX_INIT_ZERO || dtype != GRGX_BOOL, GRGX_ERR_API_MISUSE,
+               "Node initialization and bit vector type cannot be mixed");
+    GRGX_CHECK(init_kind >= GRGX_INIT_ZERO && init_kind <= GRGX_INIT_XTX, GRGX_ERR_API_MISUSE,
+               "Unexpected init value");
+    GRGX_CHECK((init_kind != GRGX_INIT_VECTOR && init_kind != GRGX_INIT_MATRIX) || init != nullptr,
+               GRGX_ERR_API_MISUSE, "init matrix is missing");
+    GRGX_CHECK(!(miss && emit_all), GRGX_ERR_API_MISUSE,
+               "The \"miss\" parameter cannot be mixed with the \"emit_all_nodes\" parameter");
+
+    if (init_kind == GRGX_INIT_XTX) {
+        {
+            std::lock_guard<std::mutex> lk(g->mu);
+            if (g->has_coals < 0) {
+                bool ok = hg.coals.size() >= n - N;
+                for (uint64_t i = 0; ok && i < n - N; i++) ok = (hg.coals[i] != COAL_NOT_SET);
+                g->has_coals = ok ? 1 : 0;
+            }
+        }
+        GRGX_CHECK(g->has_coals == 1, GRGX_ERR_API_MISUSE,
+                   "Coalescent counts not available for this GRG (init=XTX won't work)");
+    }
+    DevicePlan* dp = ensure_device_plan(g);
+
+    cudaStream_t s = static_cast<cudaStream_t>(stream_ptr);
+    const bool devPtrs = (flags & GRGX_FLAG_DEVICE_POINTERS) != 0;
+    const bool overwrite = (flags & GRGX_FLAG_OVERWRITE) != 0;
+    const long long K = static_cast<long long>(rows);
+    const Layout L = choose_layout(dtype, K, (flags & GRGX_FLAG_F32_PLAIN) != 0);
+    const size_t esz = io_size(dtype);
+    const bool down = (direction == GRGX_DIRECTION_DOWN);
+    const bool useMiss = (miss != nullptr) && dp->has_miss;
+
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    if (t_timing) {
+        for (auto& e : ev) GRGX_CUDA(cudaEventCreate(&e));
+        GRGX_CUDA(cudaEventRecord(ev[0], s));
+    }
+    uint64_t launches = 0;
+    {
+        Scratch sc(s);
+        // ---- I/O buffers -------------------------------------------------------------------
+        const size_t inBytes = rows * in_cols * esz, outBytes = rows * out_cols * esz;
+        const size_t missBytes = rows * M * esz;
+        const size_t initBytes = (init_kind == GRGX_INIT_VECTOR) ? rows * esz
+                                 : (init_kind == GRGX_INIT_MATRIX) ? rows * n * esz : 0;
+        const void* dIn = input;
+        void* dOut = output;
+        const void* dInit = init;
+        void* dMiss = useMiss ? miss : nullptr;
+        if (!devPtrs) {
+            void* a = sc.get(inBytes);
+            GRGX_CUDA(cudaMemcpyAsync(a, input, inBytes, cudaMemcpyHostToDevice, s));
+            dIn = a;
+            dOut = sc.get(outBytes);
+            if (!overwrite) GRGX_CUDA(cudaMemcpyAsync(dOut, output, outBytes, cudaMemcpyHostToDevice, s));
+            if (initBytes) {
+                void* b = sc.get(initBytes);
+                GRGX_CUDA(cudaMemcpyAsync(b, init, initBytes, cudaMemcpyHostToDevice, s));
+                dInit = b;
+            }
+            if (useMiss) {
+                dMiss = sc.get(missBytes);
+                GRGX_CUDA(cudaMemcpyAsync(dMiss, miss, missBytes, cudaMemcpyHostToDevice, s));
+            }
+        }
+        // ---- node values and the per-call scratch ---------------------------------------------
+        const size_t valBytes = static_cast<size_t>(n) * L.stride * L.ssize;
+        void* vals = sc.get(valBytes);
+        long long pieces = down ? std::max(dp->down.n_pieces, std::max(dp->seed.n_pieces, dp->miss.n_pieces))
+                                : dp->up.n_pieces;
+        void* partials = sc.get(static_cast<size_t>(pieces) * L.stride * L.asize);
+        const long long nh = down ? (dp->down.n_heavy + dp->seed.n_heavy + dp->miss.n_heavy) : dp->up.n_heavy;
+        unsigned* tickets = static_cast<unsigned*>(sc.get(static_cast<size_t>(nh) * L.ntiles * sizeof(unsigned)));
+        GRGX_CUDA(cudaMemsetAsync(tickets, 0, static_cast<size_t>(nh) * L.ntiles * sizeof(unsigned), s));
+
+        // ---- init -------------------------------------------------------------------------
+        switch (init_kind) {
+        case GRGX_INIT_VECTOR:
+            launch_init_vector(dtype, dInit, K, n, vals, L.stride, s);
+            launches++;
+            break;
+        case GRGX_INIT_MATRIX:
+            launch_load_rows(dtype, dInit, K, n, n, MAP_TABLE, 1, dp->new2old, vals, L.stride, 0, s);
+            launches++;
+            break;
+        case GRGX_INIT_XTX:
+            launch_init_xtx(dtype, dp->xtx_new, K, n, vals, L.stride, s);
+            launches++;
+            break;
+        default: GRGX_CUDA(cudaMemsetAsync(vals, 0, valBytes, s)); break;
+        }
+        const int hasInit = (init_kind != GRGX_INIT_ZERO);
+
+        if (down) {
+            // ---- DOWN seed: mutation rows, then node <- sum of its mutations ---------------------
+            unsigned* tk = tickets;
+            if (dp->seed.n_edges > 0) {
+                void* vt = sc.get(static_cast<size_t>(M) * L.stride * L.ssize);
+                launch_load_rows(dtype, dIn, K, in_cols, M, MAP_IDENT, 1, nullptr, vt, L.stride, 0, s);
+                launches++;
+                launches += launch_level(L, dp->seed, 0, vt, vals, hasInit, partials, tk, s);
+            }
+            tk += dp->seed.n_heavy * L.ntiles;
+            if (useMiss && dp->miss.n_edges > 0) {
+                void* mt = sc.get(static_cast<size_t>(M) * L.stride * L.ssize);
+                launch_load_rows(dtype, dMiss, K, M, M, MAP_IDENT, 1, nullptr, mt, L.stride, 0, s);
+                launches++;
+                launches += launch_level(L, dp->miss, 0, mt, vals, 1, partials, tk, s);
+            }
+            tk += dp->miss.n_heavy * L.ntiles;
+            if (t_timing) GRGX_CUDA(cudaEventRecord(ev[1], s));
+            for (size_t lvl = 0; lvl < dp->down.lb.size(); lvl++)
+                launches += launch_level(L, dp->down, lvl, vals, vals, 1, partials, tk, s);
+            if (t_timing) GRGX_CUDA(cudaEventRecord(ev[2], s));
+            // ---- gather samples -----------------------------------------------------------------
+            const int add = overwrite ? 0 : 1;
+            if (emit_all) {
+                launch_store_cols(dtype, vals, L.stride, K, n, MAP_TABLE, 1, dp->old2new, dOut, out_cols, add, s);
+            } else if (by_indiv) {
+                launch_store_cols(dtype, vals, L.stride, K, out_cols, MAP_FOLD, P, nullptr, dOut, out_cols, add, s);
+            } else {
+                launch_store_cols(dtype, vals, L.stride, K, out_cols, MAP_IDENT, 1, nullptr, dOut, out_cols, add, s);
+            }
+            launches++;
+        } else {
+            // ---- UP seed: samples <- input columns -------------------------------------------------
+            launch_load_rows(dtype, dIn, K, in_cols, N, by_indiv ? MAP_DIV : MAP_IDENT, P, nullptr, vals, L.stride,
+                             hasInit, s);
+            launches++;
+            if (t_timing) GRGX_CUDA(cudaEventRecord(ev[1], s));
+            for (size_t lvl = 0; lvl < dp->up.lb.size(); lvl++)
+                launches += launch_level(L, dp->up, lvl, vals, vals, hasInit, partials, tickets, s);
+            if (t_timing) GRGX_CUDA(cudaEventRecord(ev[2], s));
+            const int add = overwrite ? 0 : 1;
+            if (emit_all) {
+                launch_store_cols(dtype, vals, L.stride, K, n, MAP_TABLE, 1, dp->old2new, dOut, out_cols, add, s);
+            } else {
+                launch_store_cols(dtype, vals, L.stride, K, M, MAP_TABLE, 1, dp->mut_new, dOut, out_cols, add, s);
+                if (useMiss) {
+                    launch_store_cols(dtype, vals, L.stride, K, M, MAP_TABLE, 1, dp->miss_new, dMiss, M, 1, s);
+                    launches++;
+                }
+            }
+            launches++;
+        }
+        GRGX_CUDA(cudaGetLastError());
+        if (!devPtrs) {
+            GRGX_CUDA(cudaMemcpyAsync(output, dOut, outBytes, cudaMemcpyDeviceToHost, s));
+            if (useMiss && !down) GRGX_CUDA(cudaMemcpyAsync(miss, dMiss, missBytes, cudaMemcpyDeviceToHost, s));
+        }
+    }  // scratch released (stream-ordered)
+    if (t_timing) {
+        GRGX_CUDA(cudaEventRecord(ev[3], s));
+        GRGX_CUDA(cudaEventSynchronize(ev[3]));
+        float tot = 0, sw = 0;
+        cudaEventElapsedTime(&tot, ev[0], ev[3]);
+        cudaEventElapsedTime(&sw, ev[1], ev[2]);
+        for (auto& e : ev) cudaEventDestroy(e);
+        const DevCSR& c = down ? dp->down : dp->up;
+        t_last.total_ms = tot;
+        t_last.sweep_ms = sw;
+        t_last.launches = launches;
+        t_last.alg_bytes = static_cast<uint64_t>(c.n_edges) * (4 + static_cast<uint64_t>(K) * L.ssize) +
+                           static_cast<uint64_t>(c.n_rows) * (8 + static_cast<uint64_t>(K) * L.ssize);
+    } else {
+        t_last.launches = launches;
+    }
+    if (!devPtrs || (flags & GRGX_FLAG_SYNC)) GRGX_CUDA(cudaStreamSynchronize(s));
+}
+
+void set_timing(int enabled) { t_timing = enabled != 0; }
+grgx_timing last_timing() { return t_last; }
+
+}  // namespace grgx

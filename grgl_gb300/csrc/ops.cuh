@@ -1,0 +1,130 @@
+// Accumulation operators for the level sweep.
+//
+// Node values are stored in a "storage" type S and accumulated in a register type A:
+//   AddU32   S = A = uint32  : int32/uint32 (and int16/int8/uint16/uint8, whose sums are taken
+//                              mod 2^32 and truncated on output -- the same residues the
+//                              reference's narrow `+=` produces, internal_mult.h:42-49)
+//   AddU64   S = A = uint64  : int64/uint64, wrap-around like the reference's `+=`
+//   AddF64   S = A = double
+//   AddF32C  S = float, A = (hi, lo) pair: compensated summation with Knuth's TwoSum, the
+//            node value rounded to float once per node
+//   AddF32   S = A = float   : plain float summation
+//   XorU32   S = A = uint32  : GF(2), 32 columns per word (internal_mult.h:111-128)
+#pragma once
+#include <cstdint>
+
+namespace grgx {
+
+constexpr unsigned FULL_MASK = 0xffffffffu;
+
+struct AddU32 {
+    using S = uint32_t;
+    using A = uint32_t;
+    static __device__ __forceinline__ A zero() { return 0u; }
+    static __device__ __forceinline__ void add(A& a, S x) { a += x; }
+    static __device__ __forceinline__ void merge(A& a, const A& b) { a += b; }
+    static __device__ __forceinline__ A shfl_xor(const A& a, int m) { return __shfl_xor_sync(FULL_MASK, a, m); }
+    static __device__ __forceinline__ A shfl_up(const A& a, int d) { return __shfl_up_sync(FULL_MASK, a, d); }
+    static __device__ __forceinline__ A shfl_down(const A& a, int d) { return __shfl_down_sync(FULL_MASK, a, d); }
+    static __device__ __forceinline__ S finish(const A& a) { return a; }
+    static __device__ __forceinline__ S finish_onto(S base, const A& a) { return base + a; }
+};
+
+struct XorU32 {
+    using S = uint32_t;
+    using A = uint32_t;
+    static __device__ __forceinline__ A zero() { return 0u; }
+    static __device__ __forceinline__ void add(A& a, S x) { a ^= x; }
+    static __device__ __forceinline__ void merge(A& a, const A& b) { a ^= b; }
+    static __device__ __forceinline__ A shfl_xor(const A& a, int m) { return __shfl_xor_sync(FULL_MASK, a, m); }
+    static __device__ __forceinline__ A shfl_up(const A& a, int d) { return __shfl_up_sync(FULL_MASK, a, d); }
+    static __device__ __forceinline__ A shfl_down(const A& a, int d) { return __shfl_down_sync(FULL_MASK, a, d); }
+    static __device__ __forceinline__ S finish(const A& a) { return a; }
+    static __device__ __forceinline__ S finish_onto(S base, const A& a) { return base ^ a; }
+};
+
+struct AddU64 {
+    using S = unsigned long long;
+    using A = unsigned long long;
+    static __device__ __forceinline__ A zero() { return 0ull; }
+    static __device__ __forceinline__ void add(A& a, S x) { a += x; }
+    static __device__ __forceinline__ void merge(A& a, const A& b) { a += b; }
+    static __device__ __forceinline__ A shfl_xor(const A& a, int m) { return __shfl_xor_sync(FULL_MASK, a, m); }
+    static __device__ __forceinline__ A shfl_up(const A& a, int d) { return __shfl_up_sync(FULL_MASK, a, d); }
+    static __device__ __forceinline__ A shfl_down(const A& a, int d) { return __shfl_down_sync(FULL_MASK, a, d); }
+    static __device__ __forceinline__ S finish(const A& a) { return a; }
+    static __device__ __forceinline__ S finish_onto(S base, const A& a) { return base + a; }
+};
+
+struct AddF64 {
+    using S = double;
+    using A = double;
+    static __device__ __forceinline__ A zero() { return 0.0; }
+    static __device__ __forceinline__ void add(A& a, S x) { a += x; }
+    static __device__ __forceinline__ void merge(A& a, const A& b) { a += b; }
+    static __device__ __forceinline__ A shfl_xor(const A& a, int m) { return __shfl_xor_sync(FULL_MASK, a, m); }
+    static __device__ __forceinline__ A shfl_up(const A& a, int d) { return __shfl_up_sync(FULL_MASK, a, d); }
+    static __device__ __forceinline__ A shfl_down(const A& a, int d) { return __shfl_down_sync(FULL_MASK, a, d); }
+    static __device__ __forceinline__ S finish(const A& a) { return a; }
+    static __device__ __forceinline__ S finish_onto(S base, const A& a) { return base + a; }
+};
+
+struct AddF32 {
+    using S = float;
+    using A = float;
+    static __device__ __forceinline__ A zero() { return 0.0f; }
+    static __device__ __forceinline__ void add(A& a, S x) { a += x; }
+    static __device__ __forceinline__ void merge(A& a, const A& b) { a += b; }
+    static __device__ __forceinline__ A shfl_xor(const A& a, int m) { return __shfl_xor_sync(FULL_MASK, a, m); }
+    static __device__ __forceinline__ A shfl_up(const A& a, int d) { return __shfl_up_sync(FULL_MASK, a, d); }
+    static __device__ __forceinline__ A shfl_down(const A& a, int d) { return __shfl_down_sync(FULL_MASK, a, d); }
+    static __device__ __forceinline__ S finish(const A& a) { return a; }
+    static __device__ __forceinline__ S finish_onto(S base, const A& a) { return base + a; }
+};
+
+// Compensated float: the running sum is hi + lo with |lo| <= ulp(hi)/2.  TwoSum (Knuth,
+// TAOCP vol. 2, 4.2.2) gives the exact rounding error of each addition; the errors are
+// collected in lo and folded back when the node value is rounded to float.
+struct F32Pair {
+    float hi, lo;
+};
+
+struct AddF32C {
+    using S = float;
+    using A = F32Pair;
+    static __device__ __forceinline__ A zero() { return {0.0f, 0.0f}; }
+    static __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+        s = __fadd_rn(a, b);
+        const float bb = __fsub_rn(s, a);
+        e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    }
+    static __device__ __forceinline__ void add(A& a, S x) {
+        float s, e;
+        two_sum(a.hi, x, s, e);
+        a.hi = s;
+        a.lo = __fadd_rn(a.lo, e);
+    }
+    static __device__ __forceinline__ void merge(A& a, const A& b) {
+        float s, e;
+        two_sum(a.hi, b.hi, s, e);
+        a.hi = s;
+        a.lo = __fadd_rn(a.lo, __fadd_rn(b.lo, e));
+    }
+    static __device__ __forceinline__ A shfl_xor(const A& a, int m) {
+        return {__shfl_xor_sync(FULL_MASK, a.hi, m), __shfl_xor_sync(FULL_MASK, a.lo, m)};
+    }
+    static __device__ __forceinline__ A shfl_up(const A& a, int d) {
+        return {__shfl_up_sync(FULL_MASK, a.hi, d), __shfl_up_sync(FULL_MASK, a.lo, d)};
+    }
+    static __device__ __forceinline__ A shfl_down(const A& a, int d) {
+        return {__shfl_down_sync(FULL_MASK, a.hi, d), __shfl_down_sync(FULL_MASK, a.lo, d)};
+    }
+    static __device__ __forceinline__ S finish(const A& a) { return __fadd_rn(a.hi, a.lo); }
+    static __device__ __forceinline__ S finish_onto(S base, const A& a) {
+        A t = a;
+        add(t, base);
+        return finish(t);
+    }
+};
+
+}  // namespace grgx

@@ -1,0 +1,302 @@
+// Level plan: flattens a GRG into the device layout the sweep kernels read.
+//
+// Heights: h(v) = 0 for a node without children, else 1 + max h(child) -- the same levels the
+// reference GPU builder computes with its DFS visitor (include/grgl/cuda/gpu_grg.h:513-551).
+// Nodes are renumbered height-major, ascending original id inside a height, so samples keep
+// ids 0..N-1 and each height is one contiguous id range.
+//
+// Both traversal directions are pull-form, so no kernel needs atomics on node values:
+//   UP   value[v] = seed[v] + sum over children   (grg.h:1324-1334), heights 1..H ascending
+//   DOWN value[v] = seed[v] + sum over parents    (the push of grg.h:1312-1322 turned into a
+//        pull), heights H..0 descending, over the nodes that have parents.
+// Each direction is a CSR whose rows are laid out level by level in processing order; the
+// first edge of every row carries HEAD_BIT so a warp can find row boundaries with one ballot.
+// Every level's edge range is cut into chunks of about the same edge count; a row with more
+// edges than the chunk size is cut into pieces whose partial sums are combined in piece order.
+#include <algorithm>
+#include <atomic>
+#include <functional>
+#include <numeric>
+#include <thread>
+
+#include "grgx_internal.h"
+
+namespace grgx {
+namespace {
+
+int host_threads() {
+    unsigned t = std::thread::hardware_concurrency();
+    return t == 0 ? 4 : static_cast<int>(std::min(t, 64u));
+}
+
+void parallel_for(uint64_t n, const std::function<void(uint64_t, uint64_t, int)>& fn, int threads = 0) {
+    if (threads <= 0) threads = host_threads();
+    if (n < 65536 || threads == 1) {
+        fn(0, n, 0);
+        return;
+    }
+    std::vector<std::thread> pool;
+    for (int t = 0; t < threads; t++) {
+        const uint64_t b = n * t / threads, e = n * (t + 1) / threads;
+        pool.emplace_back([=, &fn] { fn(b, e, t); });
+    }
+    for (auto& th : pool) th.join();
+}
+
+// Chunk target: enough chunks per level to give every SM several waves of warps, never
+// fewer than 64 edges per chunk.
+constexpr int64_t kTargetChunks = 152 * 16 * 8;
+constexpr int64_t kMinChunk = 64;
+constexpr int64_t kMaxChunk = 1 << 22;
+
+void chunk_level(PullCSR& P, const std::vector<int64_t>& off, int64_t rb, int64_t re) {
+    P.level_chunk_begin.push_back(static_cast<int32_t>(P.chunks.size()));
+    const int64_t levelEdges = off[re] - off[rb];
+    P.max_level_edges = std::max(P.max_level_edges, levelEdges);
+    int64_t C = (levelEdges + kTargetChunks - 1) / kTargetChunks;
+    C = ((C + 31) / 32) * 32;
+    C = std::max(kMinChunk, std::min(kMaxChunk, C));
+    int64_t r = rb;
+    while (r < re) {
+        const int64_t deg = off[r + 1] - off[r];
+        if (deg > C) {
+            const int64_t np = (deg + C - 1) / C;
+            HeavyRow hr{};
+            hr.first_chunk = static_cast<int32_t>(P.chunks.size());
+            hr.n_pieces = static_cast<int32_t>(np);
+            hr.slot_base = P.num_pieces;
+            const int32_t hid = static_cast<int32_t>(P.heavy.size());
+            for (int64_t p = 0; p < np; p++)
+                P.chunks.push_back(Chunk{off[r] + deg * p / np, static_cast<int32_t>(r), hid});
+            P.heavy.push_back(hr);
+            P.num_pieces += np;
+            r++;
+            continue;
+        }
+        const int64_t r0 = r;
+        int64_t total = 0;
+        while (r < re) {
+            const int64_t d = off[r + 1] - off[r];
+            if (d > C || (total + d > C && r > r0)) break;
+            total += d;
+            r++;
+        }
+        P.chunks.push_back(Chunk{off[r0], static_cast<int32_t>(r0), -1});
+    }
+    P.level_chunk_end.push_back(static_cast<int32_t>(P.chunks.size()));
+}
+
+void finish_csr(PullCSR& P, const std::vector<int64_t>& off) {
+    P.chunks.push_back(Chunk{off.back(), static_cast<int32_t>(P.rows.size()), -1});
+    GRGX_CHECK(P.chunks.size() < 0x7fffffffull && P.heavy.size() < 0x7fffffffull, GRGX_ERR_UNSUPPORTED,
+               "graph too large for the chunk index");
+}
+
+// A one-level CSR from (node, source) pairs sorted by node then source.
+void single_level_csr(PullCSR& P, const std::vector<std::pair<uint32_t, uint32_t>>& pairs) {
+    std::vector<int64_t> off;
+    off.push_back(0);
+    for (size_t i = 0; i < pairs.size(); i++) {
+        if (i == 0 || pairs[i].first != pairs[i - 1].first) {
+            if (i) off.push_back(static_cast<int64_t>(i));
+            P.rows.push_back(static_cast<int32_t>(pairs[i].first));
+            P.adj.push_back(pairs[i].second | HEAD_BIT);
+        } else {
+            P.adj.push_back(pairs[i].second);
+        }
+    }
+    if (!pairs.empty()) off.push_back(static_cast<int64_t>(pairs.size()));
+    if (!P.rows.empty()) chunk_level(P, off, 0, static_cast<int64_t>(P.rows.size()));
+    finish_csr(P, off);
+}
+
+}  // namespace
+
+std::unique_ptr<HostPlan> build_plan(const HostGraph& g) {
+    const uint64_t n = g.num_nodes, N = g.num_samples;
+    GRGX_CHECK(n <= MAX_NODES, GRGX_ERR_UNSUPPORTED, "too many nodes");
+    auto plan = std::make_unique<HostPlan>();
+
+    // ---- heights -------------------------------------------------------------------------
+    std::vector<uint32_t> height(n, 0);
+    bool ordered = true;
+    for (uint64_t v = 0; v < n && ordered; v++)
+        for (uint64_t e = g.down_off[v]; e < g.down_off[v + 1]; e++)
+            if (g.down_adj[e] >= v) {
+                ordered = false;
+                break;
+            }
+    if (ordered) {
+        for (uint64_t v = 0; v < n; v++) {
+            uint32_t h = 0;
+            for (uint64_t e = g.down_off[v]; e < g.down_off[v + 1]; e++) h = std::max(h, height[g.down_adj[e]] + 1);
+            height[v] = h;
+        }
+    } else {
+        // Kahn order over parents (children first).
+        std::vector<uint32_t> pending(n), order;
+        std::vector<uint64_t> upOff(n + 1, 0);
+        for (uint64_t e = 0; e < g.num_edges(); e++) upOff[g.down_adj[e] + 1]++;
+        for (uint64_t v = 0; v < n; v++) upOff[v + 1] += upOff[v];
+        std::vector<uint32_t> upAdj(g.num_edges());
+        std::vector<uint64_t> fill(upOff.begin(), upOff.end() - 1);
+        for (uint64_t v = 0; v < n; v++) {
+            pending[v] = static_cast<uint32_t>(g.down_off[v + 1] - g.down_off[v]);
+            for (uint64_t e = g.down_off[v]; e < g.down_off[v + 1]; e++) upAdj[fill[g.down_adj[e]]++] = v;
+        }
+        order.reserve(n);
+        for (uint64_t v = 0; v < n; v++)
+            if (!pending[v]) order.push_back(v);
+        for (size_t i = 0; i < order.size(); i++) {
+            const uint32_t v = order[i];
+            for (uint64_t e = upOff[v]; e < upOff[v + 1]; e++)
+                if (--pending[upAdj[e]] == 0) order.push_back(upAdj[e]);
+        }
+        GRGX_CHECK(order.size() == n, GRGX_ERR_API_MISUSE, "GRG contains a cycle");
+        for (uint32_t v : order) {
+            uint32_t h = 0;
+            for (uint64_t e = g.down_off[v]; e < g.down_off[v + 1]; e++) h = std::max(h, height[g.down_adj[e]] + 1);
+            height[v] = h;
+        }
+    }
+    for (uint64_t s = 0; s < N; s++)
+        GRGX_CHECK(height[s] == 0, GRGX_ERR_UNSUPPORTED, "sample nodes with children are not supported");
+    uint32_t maxH = 0;
+    for (uint64_t v = 0; v < n; v++) maxH = std::max(maxH, height[v]);
+    const uint64_t L = (n == 0) ? 0 : maxH + 1;
+    plan->num_levels = L;
+
+    // ---- renumbering (stable counting sort by height) ---------------------------------------
+    plan->level_begin.assign(L + 1, 0);
+    for (uint64_t v = 0; v < n; v++) plan->level_begin[height[v] + 1]++;
+    for (uint64_t h = 0; h < L; h++) plan->level_begin[h + 1] += plan->level_begin[h];
+    plan->old2new.resize(n);
+    plan->new2old.resize(n);
+    {
+        std::vector<uint64_t> next(plan->level_begin.begin(), plan->level_begin.end());
+        for (uint64_t v = 0; v < n; v++) {
+            const uint64_t id = next[height[v]]++;
+            plan->old2new[v] = static_cast<uint32_t>(id);
+            plan->new2old[id] = static_cast<uint32_t>(v);
+        }
+    }
+    const auto& o2n = plan->old2new;
+    const auto& n2o = plan->new2old;
+
+    // ---- UP: rows = every node of heights 1..H, children in stored order --------------------
+    {
+        PullCSR& P = plan->up;
+        const uint64_t r0 = L > 1 ? plan->level_begin[1] : n;
+        const uint64_t R = n - r0;
+        P.rows.resize(R);
+        std::vector<int64_t> off(R + 1, 0);
+        for (uint64_t i = 0; i < R; i++) {
+            const uint32_t old = n2o[r0 + i];
+            P.rows[i] = static_cast<int32_t>(r0 + i);
+            off[i + 1] = off[i] + static_cast<int64_t>(g.down_off[old + 1] - g.down_off[old]);
+        }
+        P.adj.resize(off[R]);
+        parallel_for(R, [&](uint64_t b, uint64_t e, int) {
+            for (uint64_t i = b; i < e; i++) {
+                const uint32_t old = n2o[r0 + i];
+                int64_t w = off[i];
+                for (uint64_t x = g.down_off[old]; x < g.down_off[old + 1]; x++)
+                    P.adj[w++] = o2n[g.down_adj[x]] | (x == g.down_off[old] ? HEAD_BIT : 0u);
+            }
+        });
+        for (uint64_t h = 1; h < L; h++)
+            chunk_level(P, off, static_cast<int64_t>(plan->level_begin[h] - r0),
+                        static_cast<int64_t>(plan->level_begin[h + 1] - r0));
+        finish_csr(P, off);
+    }
+
+    // ---- DOWN: rows = nodes with parents, heights H..0, parents ascending by new id ---------
+    {
+        PullCSR& P = plan->down;
+        std::vector<uint64_t> pdeg(n + 1, 0);  // parent counts by new id
+        for (uint64_t e = 0; e < g.num_edges(); e++) pdeg[o2n[g.down_adj[e]]]++;
+        // Row order: heights descending, ids ascending inside a height.
+        std::vector<uint32_t> rowNode;
+        rowNode.reserve(n);
+        for (uint64_t hh = L; hh > 0; hh--) {
+            const uint64_t h = hh - 1;
+            for (uint64_t id = plan->level_begin[h]; id < plan->level_begin[h + 1]; id++)
+                if (pdeg[id]) rowNode.push_back(static_cast<uint32_t>(id));
+        }
+        const uint64_t R = rowNode.size();
+        std::vector<int64_t> rowOf(n, -1);
+        std::vector<int64_t> off(R + 1, 0);
+        for (uint64_t i = 0; i < R; i++) {
+            rowOf[rowNode[i]] = static_cast<int64_t>(i);
+            off[i + 1] = off[i] + static_cast<int64_t>(pdeg[rowNode[i]]);
+        }
+        P.rows.assign(rowNode.begin(), rowNode.end());
+        P.adj.resize(off[R]);
+        // Fill parents in ascending new id: walk parents by new id.
+        std::vector<int64_t> cursor(off.begin(), off.end() - 1);
+        for (uint64_t pid = 0; pid < n; pid++) {
+            const uint32_t old = n2o[pid];
+            for (uint64_t x = g.down_off[old]; x < g.down_off[old + 1]; x++) {
+                const int64_t row = rowOf[o2n[g.down_adj[x]]];
+                P.adj[cursor[row]++] = static_cast<uint32_t>(pid);
+            }
+        }
+        for (uint64_t i = 0; i < R; i++) P.adj[off[i]] |= HEAD_BIT;
+        // Level ranges over rows.
+        uint64_t rb = 0;
+        for (uint64_t hh = L; hh > 0; hh--) {
+            const uint64_t h = hh - 1;
+            uint64_t re = rb;
+            while (re < R && rowNode[re] >= plan->level_begin[h] && rowNode[re] < plan->level_begin[h + 1]) re++;
+            chunk_level(P, off, static_cast<int64_t>(rb), static_cast<int64_t>(re));
+            rb = re;
+        }
+        finish_csr(P, off);
+    }
+
+    // ---- mutation seeds / gathers -----------------------------------------------------------
+    plan->mut_new.assign(g.num_mutations, INVALID_NODE);
+    std::vector<std::pair<uint32_t, uint32_t>> pairs;
+    for (uint64_t m = 0; m < g.num_mutations; m++) {
+        if (g.mut_node[m] != INVALID_NODE) {
+            plan->mut_new[m] = o2n[g.mut_node[m]];
+            pairs.emplace_back(plan->mut_new[m], static_cast<uint32_t>(m));
+        }
+    }
+    std::sort(pairs.begin(), pairs.end());
+    single_level_csr(plan->seed, pairs);
+    plan->has_miss = !g.miss_node.empty();
+    plan->miss_new.assign(g.num_mutations, INVALID_NODE);
+    pairs.clear();
+    if (plan->has_miss) {
+        for (uint64_t m = 0; m < g.num_mutations; m++) {
+            if (g.miss_node[m] != INVALID_NODE) {
+                plan->miss_new[m] = o2n[g.miss_node[m]];
+                pairs.emplace_back(plan->miss_new[m], static_cast<uint32_t>(m));
+            }
+        }
+        std::sort(pairs.begin(), pairs.end());
+    }
+    single_level_csr(plan->miss, pairs);
+
+    // ---- xtx init values by new id ------------------------------------------------------------
+    plan->xtx_new.assign(n, 0);
+    plan->has_coals = true;
+    for (uint64_t id = 0; id < n; id++) {
+        const uint32_t old = n2o[id];
+        uint32_t c = 0;
+        if (old >= N) {
+            const uint64_t idx = old - N;
+            c = (idx < g.coals.size()) ? g.coals[idx] : COAL_NOT_SET;
+        }
+        if (c == COAL_NOT_SET) {
+            plan->has_coals = false;
+            plan->xtx_new[id] = COAL_NOT_SET;
+        } else {
+            plan->xtx_new[id] = c * 2u;
+        }
+    }
+    return plan;
+}
+
+}  // namespace grgx

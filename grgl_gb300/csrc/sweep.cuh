@@ -1,0 +1,250 @@
+// Level-sweep kernel: one level of the pull-form traversal.
+//
+// For every row r of the level, dst[rows[r]] (+)= sum over its edges e of src[adj[e]]: the
+// per-node edge sums of matmulSumChildrenUp / matmulSumChildrenDown (grg.h:1312-1334), one
+// level of independent nodes at a time.
+//
+// Work split: one warp per chunk (a run of whole rows, or one piece of a heavy row).  The
+// warp reads its edge ids 32 at a time (one coalesced 128-byte load) and finds row starts
+// from the HEAD_BIT of each id with a single ballot.  A row's value vector (the K columns,
+// `stride` elements padded for vector loads) is read by a group of G lanes, VW elements per
+// lane with one vector load each, so 32/G edges are gathered per sub-step.  Partial sums stay
+// in registers; at a row boundary they are combined across groups with shuffles (butterfly
+// for the finishing row, segmented scan for rows that start and end inside the sub-step) and
+// written once.  Pieces of a heavy row write partials; the last piece to finish (atomic
+// ticket) adds them up in piece order, so results do not depend on scheduling.
+#pragma once
+#include <cstdint>
+
+#include "ops.cuh"
+
+namespace grgx {
+
+struct ChunkDev {
+    long long e0;
+    int r0;
+    int heavy;
+};
+struct HeavyDev {
+    int first_chunk;
+    int n_pieces;
+    long long slot_base;
+};
+
+template <typename S> struct SweepParams {
+    const uint32_t* adj;
+    const int* rows;
+    const ChunkDev* chunks;
+    const HeavyDev* heavy;
+    long long c_begin, c_end;  // chunk range of this level
+    const S* src;              // gather source rows
+    S* dst;                    // destination rows (node values)
+    long long stride;          // elements per row (src and dst)
+    int rmw;                   // add onto the existing dst value
+    void* partials;            // Op::A per (slot, column)
+    unsigned* tickets;         // per (heavy row, column tile)
+    int ntiles;
+};
+
+template <typename S, int VW> struct Vec;
+template <> struct Vec<uint32_t, 1> { static __device__ __forceinline__ void ld(const uint32_t* p, uint32_t* v) { v[0] = __ldg(p); } static __device__ __forceinline__ void st(uint32_t* p, const uint32_t* v) { p[0] = v[0]; } };
+template <> struct Vec<uint32_t, 2> { static __device__ __forceinline__ void ld(const uint32_t* p, uint32_t* v) { uint2 t = __ldg(reinterpret_cast<const uint2*>(p)); v[0] = t.x; v[1] = t.y; } static __device__ __forceinline__ void st(uint32_t* p, const uint32_t* v) { *reinterpret_cast<uint2*>(p) = make_uint2(v[0], v[1]); } };
+template <> struct Vec<uint32_t, 4> { static __device__ __forceinline__ void ld(const uint32_t* p, uint32_t* v) { uint4 t = __ldg(reinterpret_cast<const uint4*>(p)); v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w; } static __device__ __forceinline__ void st(uint32_t* p, const uint32_t* v) { *reinterpret_cast<uint4*>(p) = make_uint4(v[0], v[1], v[2], v[3]); } };
+template <> struct Vec<float, 1> { static __device__ __forceinline__ void ld(const float* p, float* v) { v[0] = __ldg(p); } static __device__ __forceinline__ void st(float* p, const float* v) { p[0] = v[0]; } };
+template <> struct Vec<float, 2> { static __device__ __forceinline__ void ld(const float* p, float* v) { float2 t = __ldg(reinterpret_cast<const float2*>(p)); v[0] = t.x; v[1] = t.y; } static __device__ __forceinline__ void st(float* p, const float* v) { *reinterpret_cast<float2*>(p) = make_float2(v[0], v[1]); } };
+template <> struct Vec<float, 4> { static __device__ __forceinline__ void ld(const float* p, float* v) { float4 t = __ldg(reinterpret_cast<const float4*>(p)); v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w; } static __device__ __forceinline__ void st(float* p, const float* v) { *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]); } };
+template <> struct Vec<double, 1> { static __device__ __forceinline__ void ld(const double* p, double* v) { v[0] = __ldg(p); } static __device__ __forceinline__ void st(double* p, const double* v) { p[0] = v[0]; } };
+template <> struct Vec<double, 2> { static __device__ __forceinline__ void ld(const double* p, double* v) { double2 t = __ldg(reinterpret_cast<const double2*>(p)); v[0] = t.x; v[1] = t.y; } static __device__ __forceinline__ void st(double* p, const double* v) { *reinterpret_cast<double2*>(p) = make_double2(v[0], v[1]); } };
+template <> struct Vec<unsigned long long, 1> { static __device__ __forceinline__ void ld(const unsigned long long* p, unsigned long long* v) { v[0] = __ldg(p); } static __device__ __forceinline__ void st(unsigned long long* p, const unsigned long long* v) { p[0] = v[0]; } };
+template <> struct Vec<unsigned long long, 2> { static __device__ __forceinline__ void ld(const unsigned long long* p, unsigned long long* v) { ulonglong2 t = __ldg(reinterpret_cast<const ulonglong2*>(p)); v[0] = t.x; v[1] = t.y; } static __device__ __forceinline__ void st(unsigned long long* p, const unsigned long long* v) { *reinterpret_cast<ulonglong2*>(p) = make_ulonglong2(v[0], v[1]); } };
+
+// Plain (coherent) load of the current destination value, for read-modify-write.
+template <typename S, int VW> __device__ __forceinline__ void ld_plain(const S* p, S* v) {
+#pragma unroll
+    for (int i = 0; i < VW; i++) v[i] = p[i];
+}
+
+// Sum of a register vector over the 32/G groups of the warp (every group gets the result).
+template <class Op, int VW, int G> __device__ __forceinline__ void group_allreduce(typename Op::A* x) {
+#pragma unroll
+    for (int m = G; m < 32; m <<= 1) {
+#pragma unroll
+        for (int i = 0; i < VW; i++) Op::merge(x[i], Op::shfl_xor(x[i], m));
+    }
+}
+
+template <class Op, int VW>
+__device__ __forceinline__ void write_row(const SweepParams<typename Op::S>& p, long long row, int col,
+                                          const typename Op::A* tot) {
+    using S = typename Op::S;
+    const long long node = p.rows[row];
+    S* d = p.dst + node * p.stride + col;
+    S out[VW];
+    if (p.rmw) {
+        S base[VW];
+        ld_plain<S, VW>(d, base);
+#pragma unroll
+        for (int i = 0; i < VW; i++) out[i] = Op::finish_onto(base[i], tot[i]);
+    } else {
+#pragma unroll
+        for (int i = 0; i < VW; i++) out[i] = Op::finish(tot[i]);
+    }
+    Vec<S, VW>::st(d, out);
+}
+
+// L2-coherent loads for the heavy-row partials written by other warps of the same launch.
+__device__ __forceinline__ uint32_t ld_cg(const uint32_t* p) { return __ldcg(p); }
+__device__ __forceinline__ unsigned long long ld_cg(const unsigned long long* p) { return __ldcg(p); }
+__device__ __forceinline__ double ld_cg(const double* p) { return __ldcg(p); }
+__device__ __forceinline__ float ld_cg(const float* p) { return __ldcg(p); }
+__device__ __forceinline__ F32Pair ld_cg(const F32Pair* p) {
+    const float2 t = __ldcg(reinterpret_cast<const float2*>(p));
+    return {t.x, t.y};
+}
+
+template <class Op, int VW, int G>
+__global__ void __launch_bounds__(256) sweep_kernel(const SweepParams<typename Op::S> p) {
+    using S = typename Op::S;
+    using A = typename Op::A;
+    constexpr int NG = 32 / G;                 // groups per warp = edges per sub-step
+    constexpr int UNR = (G >= 8) ? 1 : 8 / G;  // 32-edge blocks per step
+    constexpr int STEPS = UNR * G;             // sub-steps per step (a multiple of 8)
+    constexpr int BATCH = 8;                   // gathers in flight per lane
+    constexpr unsigned NGMASK = (NG == 32) ? 0xffffffffu : ((1u << NG) - 1u);
+
+    const int warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    const long long c = p.c_begin + (long long)blockIdx.x * (blockDim.x >> 5) + warp;
+    if (c >= p.c_end) return;
+    const int lg = lane / G;  // group
+    const int li = lane % G;  // lane inside the group
+    const int col = blockIdx.y * (G * VW) + li * VW;
+    const bool colok = col < p.stride;
+    const unsigned upto = (2u << lg) - 1u;  // groups 0..lg
+
+    const ChunkDev ch = p.chunks[c];
+    const long long eEnd = p.chunks[c + 1].e0;
+
+    A acc[VW];
+#pragma unroll
+    for (int i = 0; i < VW; i++) acc[i] = Op::zero();
+    long long cur = ch.r0;
+    bool first = true;
+
+    for (long long base = ch.e0; base < eEnd; base += 32 * UNR) {
+        uint32_t raw[UNR];
+        unsigned heads[UNR];
+#pragma unroll
+        for (int b = 0; b < UNR; b++) {
+            const long long e = base + 32 * b + lane;
+            raw[b] = (e < eEnd) ? __ldg(p.adj + e) : 0u;
+            heads[b] = __ballot_sync(FULL_MASK, raw[b] & 0x80000000u);
+        }
+        if (first) {
+            cur = ch.r0 - (long long)(heads[0] & 1u);
+            first = false;
+        }
+#pragma unroll
+        for (int t0 = 0; t0 < STEPS; t0 += BATCH) {
+            S v[BATCH][VW];
+#pragma unroll
+            for (int u = 0; u < BATCH; u++) {
+                const int t = t0 + u;
+                const int b = t / G, s = t % G;
+                const int j = s * NG + lg;
+                const uint32_t idx = __shfl_sync(FULL_MASK, raw[b], j) & 0x7fffffffu;
+                if (base + 32 * b + j < eEnd && colok) {
+                    Vec<S, VW>::ld(p.src + (long long)idx * p.stride + col, v[u]);
+                } else {
+#pragma unroll
+                    for (int i = 0; i < VW; i++) v[u][i] = S(0);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < BATCH; u++) {
+                const int t = t0 + u;
+                const int b = t / G, s = t % G;
+                const unsigned hs = (NG == 32) ? heads[b] : ((heads[b] >> (s * NG)) & NGMASK);
+                if (hs == 0u) {
+#pragma unroll
+                    for (int i = 0; i < VW; i++) Op::add(acc[i], v[u][i]);
+                    continue;
+                }
+                const int q = __popc(hs & upto);  // rows started at or before my edge
+                const int Q = __popc(hs);
+                // 1) the current row ends in this sub-step
+                A x[VW];
+#pragma unroll
+                for (int i = 0; i < VW; i++) {
+                    x[i] = acc[i];
+                    if (q == 0) Op::add(x[i], v[u][i]);
+                }
+                group_allreduce<Op, VW, G>(x);
+                if (cur >= ch.r0 && lg == 0 && colok) write_row<Op, VW>(p, cur, col, x);
+                // 2) rows that start and end inside this sub-step: segmented scan over groups
+                if (Q > 1) {
+                    A y[VW];
+#pragma unroll
+                    for (int i = 0; i < VW; i++) {
+                        y[i] = Op::zero();
+                        if (q >= 1) Op::add(y[i], v[u][i]);
+                    }
+#pragma unroll
+                    for (int d = 1; d < NG; d <<= 1) {
+                        const int qu = __shfl_up_sync(FULL_MASK, q, d * G);
+#pragma unroll
+                        for (int i = 0; i < VW; i++) {
+                            const A tv = Op::shfl_up(y[i], d * G);
+                            if (lg >= d && qu == q) Op::merge(y[i], tv);
+                        }
+                    }
+                    const int qn = __shfl_down_sync(FULL_MASK, q, G);
+                    const bool tail = (lg == NG - 1) || (qn != q);
+                    if (tail && q >= 1 && q < Q && colok) write_row<Op, VW>(p, cur + q, col, y);
+                }
+                // 3) the last row continues into the next sub-step
+#pragma unroll
+                for (int i = 0; i < VW; i++) {
+                    acc[i] = Op::zero();
+                    if (q == Q) Op::add(acc[i], v[u][i]);
+                }
+                cur += Q;
+            }
+        }
+    }
+
+    group_allreduce<Op, VW, G>(acc);
+    if (ch.heavy < 0) {
+        if (lg == 0 && colok) write_row<Op, VW>(p, cur, col, acc);
+        return;
+    }
+    // Piece of a heavy row: publish the partial, then the last piece combines all of them.
+    const HeavyDev hr = p.heavy[ch.heavy];
+    const long long piece = c - hr.first_chunk;
+    A* part = reinterpret_cast<A*>(p.partials);
+    if (lg == 0 && colok) {
+#pragma unroll
+        for (int i = 0; i < VW; i++) part[(hr.slot_base + piece) * p.stride + col + i] = acc[i];
+    }
+    __threadfence();
+    __syncwarp();
+    unsigned ticket = 0;
+    if (lane == 0) ticket = atomicAdd(p.tickets + (long long)ch.heavy * p.ntiles + blockIdx.y, 1u);
+    ticket = __shfl_sync(FULL_MASK, ticket, 0);
+    if (ticket != (unsigned)hr.n_pieces - 1u) return;
+    __threadfence();
+    A sum[VW];
+#pragma unroll
+    for (int i = 0; i < VW; i++) sum[i] = Op::zero();
+    if (colok) {
+        for (int pc = lg; pc < hr.n_pieces; pc += NG) {
+            const A* src = part + (hr.slot_base + pc) * p.stride + col;
+#pragma unroll
+            for (int i = 0; i < VW; i++) Op::merge(sum[i], ld_cg(src + i));
+        }
+    }
+    group_allreduce<Op, VW, G>(sum);
+    if (lg == 0 && colok) write_row<Op, VW>(p, cur, col, sum);
+}
+
+}  // namespace grgx

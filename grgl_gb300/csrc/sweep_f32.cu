@@ -1,0 +1,8 @@
+// Sweep kernel instances for the AddF32 accumulation operator.
+#include "sweep_inst.cuh"
+
+namespace grgx {
+void launch_sweep_f32(const SweepParams<float>& p, int vw, int g, dim3 grid, cudaStream_t s) {
+    GRGX_SWEEP_DISPATCH4(AddF32)
+}
+}  // namespace grgx

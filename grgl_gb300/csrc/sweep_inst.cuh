@@ -1,0 +1,34 @@
+// Instantiation helper: a dispatcher from runtime (VW, G) to the sweep_kernel template.
+#pragma once
+#include <stdexcept>
+
+#include "launch.h"
+
+#define GRGX_SWEEP_CASE(OP, VWV, GV)                                                  \
+    if (vw == VWV && g == GV) {                                                       \
+        sweep_kernel<OP, VWV, GV><<<grid, 256, 0, s>>>(p);                            \
+        return;                                                                       \
+    }
+
+// 4-byte storage: (1,1), (2,1), (4, 1..32)
+#define GRGX_SWEEP_DISPATCH4(OP)                                                      \
+    GRGX_SWEEP_CASE(OP, 1, 1)                                                         \
+    GRGX_SWEEP_CASE(OP, 2, 1)                                                         \
+    GRGX_SWEEP_CASE(OP, 4, 1)                                                         \
+    GRGX_SWEEP_CASE(OP, 4, 2)                                                         \
+    GRGX_SWEEP_CASE(OP, 4, 4)                                                         \
+    GRGX_SWEEP_CASE(OP, 4, 8)                                                         \
+    GRGX_SWEEP_CASE(OP, 4, 16)                                                        \
+    GRGX_SWEEP_CASE(OP, 4, 32)                                                        \
+    throw std::runtime_error("unsupported sweep shape");
+
+// 8-byte storage: (1,1), (2, 1..32)
+#define GRGX_SWEEP_DISPATCH8(OP)                                                      \
+    GRGX_SWEEP_CASE(OP, 1, 1)                                                         \
+    GRGX_SWEEP_CASE(OP, 2, 1)                                                         \
+    GRGX_SWEEP_CASE(OP, 2, 2)                                                         \
+    GRGX_SWEEP_CASE(OP, 2, 4)                                                         \
+    GRGX_SWEEP_CASE(OP, 2, 8)                                                         \
+    GRGX_SWEEP_CASE(OP, 2, 16)                                                        \
+    GRGX_SWEEP_CASE(OP, 2, 32)                                                        \
+    throw std::runtime_error("unsupported sweep shape");

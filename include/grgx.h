@@ -1,0 +1,151 @@
+/*
+ * grgx -- GB300-native GRG matrix multiplication, C ABI.
+ *
+ * Drop-in boundary for GRGL's graph matrix multiplication.  Each entry point names the
+ * reference interface (aprilweilab/grgl 2.10) it stands in for.  Plain pointers and sizes
+ * only; no C++ or framework types cross this boundary, and no exception escapes it: every
+ * call returns a grgx_status, with a human-readable message from grgx_last_error() (the
+ * reference's own message text where the reference has one).
+ *
+ * Threading: a graph handle is immutable after creation; any number of threads may call
+ * grgx_matmul on one handle at once.  Each call allocates its own scratch from the device's
+ * stream-ordered memory pool, on the stream it is given.
+ */
+#ifndef GRGX_H
+#define GRGX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct grgx_graph grgx_graph;
+
+typedef enum {
+    GRGX_OK = 0,
+    GRGX_ERR_API_MISUSE = 1, /* reference ApiMisuseFailure (common.h:45-58) -> RuntimeError */
+    GRGX_ERR_CUDA = 2,       /* a CUDA runtime call failed */
+    GRGX_ERR_OUT_OF_MEMORY = 3,
+    GRGX_ERR_BAD_FILE = 4,   /* reference SerializationFailure / BadInputFileFailure */
+    GRGX_ERR_UNSUPPORTED = 5,
+    GRGX_ERR_NO_DEVICE = 6,
+    GRGX_ERR_TIMEOUT = 7
+} grgx_status;
+
+/* TraversalDirection values (include/grgl/visitor.h:26). */
+typedef enum { GRGX_DIRECTION_DOWN = 1, GRGX_DIRECTION_UP = 2 } grgx_direction;
+
+/* Element types accepted by pygrgl.matmul (_grgl.cpp:205-238). */
+typedef enum {
+    GRGX_F64 = 0,
+    GRGX_F32 = 1,
+    GRGX_I64 = 2,
+    GRGX_I32 = 3,
+    GRGX_I16 = 4,
+    GRGX_I8 = 5,
+    GRGX_U64 = 6,
+    GRGX_U32 = 7,
+    GRGX_U16 = 8,
+    GRGX_U8 = 9,
+    GRGX_BOOL = 10 /* GF(2): one byte per value (0/1) in and out, XOR accumulation */
+} grgx_dtype;
+
+/* GRG::NodeInitEnum (include/grgl/grg.h:646-651). */
+typedef enum { GRGX_INIT_ZERO = 0, GRGX_INIT_VECTOR = 1, GRGX_INIT_MATRIX = 2, GRGX_INIT_XTX = 3 } grgx_init;
+
+/* grgx_matmul flags. */
+#define GRGX_FLAG_DEVICE_POINTERS 0x1u /* input/output/init/miss are device pointers */
+#define GRGX_FLAG_F32_PLAIN 0x2u       /* f32: plain (uncompensated) accumulation */
+#define GRGX_FLAG_SYNC 0x4u            /* wait for the stream before returning */
+#define GRGX_FLAG_OVERWRITE 0x8u       /* write the output instead of adding to it */
+
+typedef struct {
+    uint64_t num_nodes;
+    uint64_t num_edges;
+    uint64_t num_samples;
+    uint64_t num_mutations;
+    uint64_t ploidy;
+    uint64_t num_levels;
+    uint64_t has_missing; /* graph carries missingness nodes */
+    uint64_t has_coals;   /* every non-sample node has a coalescence count (init=xtx works) */
+    uint64_t device_bytes; /* resident plan size once uploaded (0 before) */
+} grgx_graph_info;
+
+/* Message for the last failing call on this thread ("" if none). */
+const char* grgx_last_error(void);
+
+/* Library version string. */
+const char* grgx_version(void);
+
+/* Replaces grgl::loadImmutableGRG (src/serialize.cpp:923-937, readImmutableGrg :815-890):
+ * reads a .grg file (format 5.x) into a host graph.  Fails with GRGX_ERR_BAD_FILE on a
+ * malformed file, with the reference's message text. */
+grgx_status grgx_graph_load(const char* path, grgx_graph** out);
+
+/* Builds a graph from the arrays a CSRGRG holds (include/grgl/grg.h:1232-1303): the down-edge
+ * CSR (children of node v are down_adj[down_off[v] .. down_off[v+1])), the mutation -> node
+ * map (getNodesAndMutations, grg.h:406-415; 0x7fffffff = unmapped), optional missingness
+ * nodes (NULL = none) and optional coalescence counts of the non-sample nodes
+ * (getNumIndividualCoals, grg.h:743-747; NULL = not set).  Arrays are copied. */
+grgx_status grgx_graph_from_csr(uint64_t num_nodes, uint64_t num_samples, uint64_t ploidy,
+                                const uint64_t* down_off, const uint32_t* down_adj, uint64_t num_mutations,
+                                const uint32_t* mut_node, const uint32_t* miss_node, const uint32_t* coals,
+                                grgx_graph** out);
+
+/* Seeded window-tree GRG: one Kingman coalescent tree over all samples per window of
+ * `window` consecutive variants, mutations placed on branches in proportion to branch
+ * length, each tree collapsed to its mutation nodes (no reference counterpart: the
+ * synthetic-workload producer; `threads` <= 0 means all host cores). */
+grgx_status grgx_graph_generate(uint64_t num_samples, uint64_t num_mutations, uint64_t seed, uint32_t window,
+                                int threads, grgx_graph** out);
+
+void grgx_graph_destroy(grgx_graph* g);
+
+grgx_status grgx_graph_info_get(const grgx_graph* g, grgx_graph_info* out);
+
+/* Copies of the host arrays (for checkers and exporters): sizes from grgx_graph_info_get;
+ * miss_node / coals may be NULL to skip them. */
+grgx_status grgx_graph_export(const grgx_graph* g, uint64_t* down_off, uint32_t* down_adj, uint32_t* mut_node,
+                              uint32_t* miss_node, uint32_t* coals);
+
+/* Builds the level plan and copies it to the current device (done implicitly by the first
+ * grgx_matmul; explicit here so callers can keep it out of timed regions). */
+grgx_status grgx_graph_upload(grgx_graph* g);
+
+/* Replaces GRG::matrixMultiplication<IOType, NodeValueType, useBitVector>
+ * (include/grgl/grg.h:1341-1517, argument for argument) and, through it, GRG::matMul
+ * (grg.h:705-716) and the pygrgl.matmul / dot_product bindings (_grgl.cpp:80-241):
+ *   input       K x input_cols row-major (K = input_rows)
+ *   output      output_size = K x output_cols row-major; ADDED to, like the reference
+ *               (callers zero it for a plain product)
+ *   init        init_kind VECTOR: K values; MATRIX: K x num_nodes; else ignored
+ *   miss        K x num_mutations; an input in DOWN, an in/out accumulator in UP; NULL = none
+ *   stream      cudaStream_t (NULL = legacy default stream)
+ * With GRGX_FLAG_DEVICE_POINTERS the buffers are device pointers and the call is
+ * asynchronous on `stream`; otherwise they are host pointers and the call returns when the
+ * output (and miss) have been written back.  Validation and messages follow
+ * validateMatMulInputs (internal_mult.h:130-158). */
+grgx_status grgx_matmul(grgx_graph* g, grgx_dtype dtype, const void* input, uint64_t input_cols,
+                        uint64_t input_rows, grgx_direction direction, void* output, uint64_t output_size,
+                        int emit_all_nodes, int by_individual, const void* init, grgx_init init_kind, void* miss,
+                        uint32_t flags, void* stream);
+
+/* Device-time breakdown of the last grgx_matmul made by this thread with timing enabled. */
+typedef struct {
+    float total_ms;     /* seed + sweep + gather, CUDA events */
+    float sweep_ms;     /* level sweep only */
+    uint64_t launches;  /* kernels launched by the call */
+    uint64_t alg_bytes; /* algorithmic bytes of the sweep (edge ids + offsets + one row per edge + one row per node) */
+} grgx_timing;
+
+/* Enables per-call CUDA-event timing on this thread (adds a stream sync per call). */
+void grgx_set_timing(int enabled);
+grgx_status grgx_last_timing(grgx_timing* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GRGX_H */
