@@ -12,7 +12,7 @@ from pathlib import Path
 LIB_PATH = Path(__file__).resolve().parent / "libgrgx.so"
 
 OK, ERR_API_MISUSE, ERR_CUDA, ERR_OOM, ERR_BAD_FILE, ERR_UNSUPPORTED, ERR_NO_DEVICE, ERR_TIMEOUT = range(8)
-FLAG_DEVICE_POINTERS, FLAG_F32_PLAIN, FLAG_SYNC, FLAG_OVERWRITE = 0x1, 0x2, 0x4, 0x8
+FLAG_DEVICE_POINTERS, FLAG_F32_PLAIN, FLAG_SYNC, FLAG_OVERWRITE, FLAG_F64_NATIVE = 0x1, 0x2, 0x4, 0x8, 0x10
 
 # Every symbol include/grgx.h declares, with its ctypes signature.
 c_graph_p = ctypes.c_void_p

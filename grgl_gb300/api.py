@@ -203,15 +203,21 @@ def _torch_dtype_to_np(t):
             torch.int16: np.int16, torch.int8: np.int8, torch.uint8: np.uint8, torch.bool: np.bool_}.get(t)
 
 
+def _flags(f32_compensated: bool, f64_native: bool) -> int:
+    return ((0 if f32_compensated else _lib.FLAG_F32_PLAIN) | (_lib.FLAG_F64_NATIVE if f64_native else 0))
+
+
 def matmul(grg: GRG, input, direction, emit_all_nodes: bool = False, by_individual: bool = False, init=None,
-           miss=None, *, f32_compensated: bool = True):
+           miss=None, *, f32_compensated: bool = True, f64_native: bool = False):
     """pygrgl.matmul on the GPU (reference: _grgl.cpp:187-241, grg.h:1341-1517).
 
     ``f32_compensated`` (float32 only, default True) accumulates with TwoSum compensation; False
-    gives plain float summation.
+    gives plain float summation.  ``f64_native`` (float64 only, default False) accumulates on the
+    FP64 pipe instead of as scaled float pairs with double folds (same tolerance, slower on GB300).
     """
     if _is_torch_cuda(input):
-        return _matmul_device(grg, input, direction, emit_all_nodes, by_individual, init, miss, f32_compensated)
+        return _matmul_device(grg, input, direction, emit_all_nodes, by_individual, init, miss,
+                              _flags(f32_compensated, f64_native))
     direction = TraversalDirection(int(direction))
     if not isinstance(input, np.ndarray):
         raise RuntimeError(f"Unsupported numpy dtype: {np.asarray(input).dtype}")
@@ -226,7 +232,7 @@ def matmul(grg: GRG, input, direction, emit_all_nodes: bool = False, by_individu
     init_kind, init_arr = _parse_init(grg, init, arr.dtype, rows, code == 10)
     miss_arr = _parse_miss(miss, arr.dtype, rows, cols, out_cols, direction, emit_all_nodes)
     out = np.empty((rows, out_cols), dtype=arr.dtype)
-    flags = _lib.FLAG_OVERWRITE | (0 if f32_compensated else _lib.FLAG_F32_PLAIN)
+    flags = _lib.FLAG_OVERWRITE | _flags(f32_compensated, f64_native)
     _lib.check(_lib.lib().grgx_matmul(grg._h, code, arr.ctypes.data, cols, rows, int(direction), out.ctypes.data,
                                       out.size, int(bool(emit_all_nodes)), int(bool(by_individual)),
                                       init_arr.ctypes.data if init_arr is not None else None, init_kind,
@@ -287,7 +293,7 @@ def _parse_miss(miss, dtype, rows, cols, out_cols, direction, emit_all):
     return miss if miss.flags.c_contiguous else np.ascontiguousarray(miss)
 
 
-def _matmul_device(grg, x, direction, emit_all, by_indiv, init, miss, f32_compensated):
+def _matmul_device(grg, x, direction, emit_all, by_indiv, init, miss, extra_flags):
     import torch
 
     direction = TraversalDirection(int(direction))
@@ -307,7 +313,7 @@ def _matmul_device(grg, x, direction, emit_all, by_indiv, init, miss, f32_compen
     _check(miss_t is None or _is_torch_cuda(miss_t), '"miss" must be a CUDA tensor when the input is one')
     out = torch.empty((rows, out_cols), dtype=x.dtype, device=x.device)
     stream = torch.cuda.current_stream(x.device).cuda_stream
-    flags = _lib.FLAG_OVERWRITE | _lib.FLAG_DEVICE_POINTERS | (0 if f32_compensated else _lib.FLAG_F32_PLAIN)
+    flags = _lib.FLAG_OVERWRITE | _lib.FLAG_DEVICE_POINTERS | extra_flags
     with torch.cuda.device(x.device):
         _lib.check(_lib.lib().grgx_matmul(grg._h, code, x.data_ptr(), cols, rows, int(direction), out.data_ptr(),
                                           out.numel(), int(bool(emit_all)), int(bool(by_indiv)),

@@ -1,0 +1,194 @@
+// Seed and gather kernels for float64 carried as scaled float pairs (AddF64S, ops.cuh).
+//
+// Each input row k is scaled by the exact power of two 2^-e_k (e_k = exponent of the row's
+// largest finite magnitude, clamped to the normal range) before it is split into hi + lo floats,
+// and the outputs are scaled back by 2^e_k; scaling by powers of two is exact, so the only
+// rounding is the split's 2^-48 relative representation error.
+#include <cstdint>
+
+#include "launch.h"
+
+namespace grgx {
+namespace {
+
+constexpr uint32_t kInvalid = 0x7fffffffu;
+constexpr unsigned long long kExpMask = 0x7ff0000000000000ull;
+
+__device__ __forceinline__ int row_exp(const unsigned long long* rowmax, long long k) {
+    const unsigned long long b = rowmax[k];
+    if (b == 0) return 0;
+    int e = static_cast<int>((b >> 52) & 0x7ff) - 1023;
+    return e < -1022 ? -1022 : (e > 1022 ? 1022 : e);
+}
+
+// 2^e for e in [-1022, 1023], built from its bit pattern (exact).
+__device__ __forceinline__ double pow2(int e) {
+    return __longlong_as_double(static_cast<long long>(e + 1023) << 52);
+}
+
+__global__ void fill_u64_kernel(unsigned long long* p, long long n, unsigned long long v) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        p[i] = v;
+}
+
+__global__ void rowmax_kernel(const double* __restrict__ src, long long K, long long ld, long long cols,
+                              unsigned long long* __restrict__ rowmax) {
+    __shared__ unsigned long long red[8];
+    for (long long k = blockIdx.y; k < K; k += gridDim.y) {
+        unsigned long long m = 0;
+        for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < cols;
+             c += (long long)gridDim.x * blockDim.x) {
+            const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(src[k * ld + c])) &
+                                         0x7fffffffffffffffull;
+            if ((b & kExpMask) != kExpMask && b > m) m = b;  // finite only
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long t = __shfl_xor_sync(0xffffffffu, m, o);
+            m = t > m ? t : m;
+        }
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned long long r = 0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); w++) r = red[w] > r ? red[w] : r;
+            if (r) atomicMax(rowmax + k, r);
+        }
+        __syncthreads();
+    }
+}
+
+__device__ __forceinline__ DF split_scaled(double x, int e) { return AddF64S::split(x * pow2(-e)); }
+
+__global__ void load_rows_df_kernel(const double* __restrict__ src, long long K, long long ld, long long R, int mode,
+                                    long long div, const uint32_t* __restrict__ tab, DF* __restrict__ dst,
+                                    long long stride, int add, const unsigned long long* __restrict__ rowmax) {
+    __shared__ DF tile[32][33];
+    const long long i0 = (long long)blockIdx.x * 32, k0 = (long long)blockIdx.y * 32;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const long long i = i0 + tx;
+    long long colIdx = -1;
+    if (i < R) colIdx = (mode == MAP_DIV) ? i / div : (mode == MAP_TABLE ? (long long)tab[i] : i);
+#pragma unroll
+    for (int j = ty; j < 32; j += 8) {
+        const long long k = k0 + j;
+        tile[j][tx] = (k < K && colIdx >= 0) ? split_scaled(src[k * ld + colIdx], row_exp(rowmax, k)) : DF{0.f, 0.f};
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = ty; j < 32; j += 8) {
+        const long long r = i0 + j, k = k0 + tx;
+        if (r < R && k < stride) {
+            DF* d = dst + r * stride + k;
+            if (add) {
+                if (k < K) *d = AddF64S::split(AddF64S::value(*d) + AddF64S::value(tile[tx][j]));
+            } else {
+                *d = tile[tx][j];
+            }
+        }
+    }
+}
+
+__global__ void store_cols_df_kernel(const DF* __restrict__ vals, long long stride, long long K, long long C,
+                                     int mode, long long fold, const uint32_t* __restrict__ tab,
+                                     double* __restrict__ out, long long ld, int add,
+                                     const unsigned long long* __restrict__ rowmax) {
+    __shared__ double tile[32][33];
+    const long long c0 = (long long)blockIdx.x * 32, k0 = (long long)blockIdx.y * 32;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+#pragma unroll
+    for (int j = ty; j < 32; j += 8) {
+        const long long c = c0 + j, k = k0 + tx;
+        double v = 0.0;
+        if (c < C && k < K) {
+            if (mode == MAP_FOLD) {
+                for (long long p = 0; p < fold; p++) v += AddF64S::value(vals[(c * fold + p) * stride + k]);
+            } else {
+                const long long node = (mode == MAP_TABLE) ? (long long)tab[c] : c;
+                if (node != (long long)kInvalid) v = AddF64S::value(vals[node * stride + k]);
+            }
+            v *= pow2(row_exp(rowmax, k));
+        }
+        tile[j][tx] = v;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = ty; j < 32; j += 8) {
+        const long long k = k0 + j, c = c0 + tx;
+        if (k < K && c < C) {
+            double* o = out + k * ld + c;
+            *o = add ? (*o + tile[tx][j]) : tile[tx][j];
+        }
+    }
+}
+
+__global__ void init_vector_df_kernel(const double* __restrict__ init, long long K, long long n, DF* __restrict__ vals,
+                                      long long stride, const unsigned long long* __restrict__ rowmax) {
+    const long long total = n * stride;
+    for (long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x; x < total;
+         x += (long long)gridDim.x * blockDim.x) {
+        const long long k = x % stride;
+        vals[x] = (k < K) ? split_scaled(init[k], row_exp(rowmax, k)) : DF{0.f, 0.f};
+    }
+}
+
+__global__ void init_xtx_df_kernel(const uint32_t* __restrict__ xtx, long long K, long long n, DF* __restrict__ vals,
+                                   long long stride, const unsigned long long* __restrict__ rowmax) {
+    const long long total = n * stride;
+    for (long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x; x < total;
+         x += (long long)gridDim.x * blockDim.x) {
+        const long long k = x % stride, v = x / stride;
+        vals[x] = (k < K) ? split_scaled(static_cast<double>(xtx[v]), row_exp(rowmax, k)) : DF{0.f, 0.f};
+    }
+}
+
+unsigned grid_for(long long total) {
+    long long b = (total + 255) / 256;
+    if (b > 152 * 32) b = 152 * 32;
+    return (unsigned)(b < 1 ? 1 : b);
+}
+
+}  // namespace
+
+void launch_fill_u64(unsigned long long* p, long long n, unsigned long long v, cudaStream_t s) {
+    if (n <= 0) return;
+    fill_u64_kernel<<<grid_for(n), 256, 0, s>>>(p, n, v);
+}
+
+void launch_rowmax(const double* src, long long K, long long ld, long long cols, unsigned long long* rowmax,
+                   cudaStream_t s) {
+    if (K <= 0 || cols <= 0) return;
+    long long bx = (cols + 256 * 8 - 1) / (256 * 8);
+    if (bx > 1024) bx = 1024;
+    const long long by = K < 65535 ? K : 65535;
+    rowmax_kernel<<<dim3((unsigned)bx, (unsigned)by), 256, 0, s>>>(src, K, ld, cols, rowmax);
+}
+
+void launch_load_rows_df(const double* src, long long K, long long ld, long long R, int mode, long long div,
+                         const uint32_t* tab, void* dst, long long stride, int add,
+                         const unsigned long long* rowmax, cudaStream_t s) {
+    if (R <= 0) return;
+    const dim3 grid((unsigned)((R + 31) / 32), (unsigned)((stride + 31) / 32));
+    load_rows_df_kernel<<<grid, dim3(32, 8), 0, s>>>(src, K, ld, R, mode, div, tab, static_cast<DF*>(dst), stride,
+                                                     add, rowmax);
+}
+
+void launch_store_cols_df(const void* vals, long long stride, long long K, long long C, int mode, long long fold,
+                          const uint32_t* tab, double* out, long long ld, int add,
+                          const unsigned long long* rowmax, cudaStream_t s) {
+    if (C <= 0 || K <= 0) return;
+    const dim3 grid((unsigned)((C + 31) / 32), (unsigned)((K + 31) / 32));
+    store_cols_df_kernel<<<grid, dim3(32, 8), 0, s>>>(static_cast<const DF*>(vals), stride, K, C, mode, fold, tab,
+                                                      out, ld, add, rowmax);
+}
+
+void launch_init_vector_df(const double* init, long long K, long long n, void* vals, long long stride,
+                           const unsigned long long* rowmax, cudaStream_t s) {
+    init_vector_df_kernel<<<grid_for(n * stride), 256, 0, s>>>(init, K, n, static_cast<DF*>(vals), stride, rowmax);
+}
+
+void launch_init_xtx_df(const uint32_t* xtx, long long K, long long n, void* vals, long long stride,
+                        const unsigned long long* rowmax, cudaStream_t s) {
+    init_xtx_df_kernel<<<grid_for(n * stride), 256, 0, s>>>(xtx, K, n, static_cast<DF*>(vals), stride, rowmax);
+}
+
+}  // namespace grgx

@@ -9,15 +9,16 @@
 namespace grgx {
 
 // Storage/accumulation kinds (see ops.cuh).
-enum class Kind { U32, U64, F64, F32C, F32, XOR };
+enum class Kind { U32, U64, F64, F32C, F32, XOR, F64S };
 
 // One level (or seed pass) of the sweep; VW elements per lane, G lanes per row.
-void launch_sweep_u32(const SweepParams<uint32_t>& p, int vw, int g, dim3 grid, cudaStream_t s);
-void launch_sweep_xor(const SweepParams<uint32_t>& p, int vw, int g, dim3 grid, cudaStream_t s);
-void launch_sweep_u64(const SweepParams<unsigned long long>& p, int vw, int g, dim3 grid, cudaStream_t s);
-void launch_sweep_f64(const SweepParams<double>& p, int vw, int g, dim3 grid, cudaStream_t s);
-void launch_sweep_f32c(const SweepParams<float>& p, int vw, int g, dim3 grid, cudaStream_t s);
-void launch_sweep_f32(const SweepParams<float>& p, int vw, int g, dim3 grid, cudaStream_t s);
+void launch_sweep_u32(const SweepParams<uint32_t>& p, int vw, int g, dim3 grid, int sms, cudaStream_t s);
+void launch_sweep_xor(const SweepParams<uint32_t>& p, int vw, int g, dim3 grid, int sms, cudaStream_t s);
+void launch_sweep_u64(const SweepParams<unsigned long long>& p, int vw, int g, dim3 grid, int sms, cudaStream_t s);
+void launch_sweep_f64(const SweepParams<double>& p, int vw, int g, dim3 grid, int sms, cudaStream_t s);
+void launch_sweep_f32c(const SweepParams<float>& p, int vw, int g, dim3 grid, int sms, cudaStream_t s);
+void launch_sweep_f32(const SweepParams<float>& p, int vw, int g, dim3 grid, int sms, cudaStream_t s);
+void launch_sweep_f64s(const SweepParams<DF>& p, int vw, int g, dim3 grid, int sms, cudaStream_t s);
 
 // Column-map modes of the transposing loads/stores.
 enum MapMode { MAP_IDENT = 0, MAP_DIV = 1, MAP_TABLE = 2, MAP_FOLD = 3 };
@@ -37,5 +38,23 @@ void launch_init_vector(int dtype, const void* init, long long K, long long n, v
                         cudaStream_t s);
 void launch_init_xtx(int dtype, const uint32_t* xtx, long long K, long long n, void* vals, long long stride,
                      cudaStream_t s);
+
+// ---- float64 as scaled float pairs (AddF64S) ----------------------------------------------
+// rowmax[k] = max over finite |x| of row k, as IEEE bits (0 for an all-zero row); callers
+// fill it first (0, or a floor such as the largest XTX init value) and may fold several
+// matrices into it.  Row k is scaled by 2^-e_k with e_k the exponent of rowmax[k].
+void launch_fill_u64(unsigned long long* p, long long n, unsigned long long v, cudaStream_t s);
+void launch_rowmax(const double* src, long long K, long long ld, long long cols, unsigned long long* rowmax,
+                   cudaStream_t s);
+void launch_load_rows_df(const double* src, long long K, long long ld, long long R, int mode, long long div,
+                         const uint32_t* tab, void* dst, long long stride, int add,
+                         const unsigned long long* rowmax, cudaStream_t s);
+void launch_store_cols_df(const void* vals, long long stride, long long K, long long C, int mode, long long fold,
+                          const uint32_t* tab, double* out, long long ld, int add,
+                          const unsigned long long* rowmax, cudaStream_t s);
+void launch_init_vector_df(const double* init, long long K, long long n, void* vals, long long stride,
+                           const unsigned long long* rowmax, cudaStream_t s);
+void launch_init_xtx_df(const uint32_t* xtx, long long K, long long n, void* vals, long long stride,
+                        const unsigned long long* rowmax, cudaStream_t s);
 
 }  // namespace grgx

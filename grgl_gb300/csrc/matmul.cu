@@ -51,6 +51,7 @@ struct DevicePlan {
     uint64_t num_levels = 0;
     bool has_coals = false;
     bool has_miss = false;
+    double xtx_max = 0.0;  // largest XTX init value (2 * coalescences)
     std::vector<void*> allocs;
 };
 
@@ -121,17 +122,17 @@ long long next_pow2(long long x) {
     return p;
 }
 
-Layout choose_layout(int dtype, long long K, bool plainF32) {
+Layout choose_layout(int dtype, long long K, bool plainF32, bool nativeF64) {
     Layout L{};
     long long base = K;
     switch (dtype) {
-    case GRGX_F64: L.kind = Kind::F64; L.ssize = 8; break;
+    case GRGX_F64: L.kind = nativeF64 ? Kind::F64 : Kind::F64S; L.ssize = 8; break;
     case GRGX_F32: L.kind = plainF32 ? Kind::F32 : Kind::F32C; L.ssize = 4; break;
     case GRGX_I64: case GRGX_U64: L.kind = Kind::U64; L.ssize = 8; break;
     case GRGX_BOOL: L.kind = Kind::XOR; L.ssize = 4; base = (K + 31) / 32; break;
     default: L.kind = Kind::U32; L.ssize = 4; break;
     }
-    L.asize = (L.kind == Kind::F32C) ? 8 : L.ssize;
+    L.asize = (L.kind == Kind::F32C) ? 8 : (L.kind == Kind::F64S ? 24 : L.ssize);
     const int maxVw = 16 / L.ssize;
     if (base == 1) {
         L.stride = 1; L.vw = 1; L.g = 1; L.ntiles = 1;
@@ -166,9 +167,20 @@ struct Scratch {
 thread_local bool t_timing = false;
 thread_local grgx_timing t_last{};
 
+int sm_count() {
+    static int sms = 0;
+    if (sms == 0) {
+        int dev = 0, v = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+        sms = v > 0 ? v : 1;
+    }
+    return sms;
+}
+
 template <typename S>
 SweepParams<S> make_params(const DevCSR& c, long long cb, long long ce, const void* src, void* dst, long long stride,
-                           int rmw, void* partials, unsigned* tickets, int ntiles) {
+                           int rmw, void* partials, unsigned* tickets, unsigned* work, int ntiles) {
     SweepParams<S> p;
     p.adj = c.adj;
     p.rows = c.rows;
@@ -182,41 +194,48 @@ SweepParams<S> make_params(const DevCSR& c, long long cb, long long ce, const vo
     p.rmw = rmw;
     p.partials = partials;
     p.tickets = tickets;
+    p.work = work;
     p.ntiles = ntiles;
     return p;
 }
 
 // Launches one level of a CSR; returns the number of kernels launched (0 or 1).
+// `work` points at L.ntiles zeroed counters owned by this launch.
 int launch_level(const Layout& L, const DevCSR& c, size_t level, const void* src, void* dst, int rmw,
-                 void* partials, unsigned* tickets, cudaStream_t s) {
+                 void* partials, unsigned* tickets, unsigned* work, cudaStream_t s) {
     const long long cb = c.lb[level], ce = c.le[level];
     if (ce <= cb) return 0;
     const dim3 grid(static_cast<unsigned>((ce - cb + 7) / 8), static_cast<unsigned>(L.ntiles));
+    const int sms = sm_count();
     switch (L.kind) {
     case Kind::U32:
-        launch_sweep_u32(make_params<uint32_t>(c, cb, ce, src, dst, L.stride, rmw, partials, tickets, L.ntiles),
-                         L.vw, L.g, grid, s);
+        launch_sweep_u32(make_params<uint32_t>(c, cb, ce, src, dst, L.stride, rmw, partials, tickets, work, L.ntiles),
+                         L.vw, L.g, grid, sms, s);
         break;
     case Kind::XOR:
-        launch_sweep_xor(make_params<uint32_t>(c, cb, ce, src, dst, L.stride, rmw, partials, tickets, L.ntiles),
-                         L.vw, L.g, grid, s);
+        launch_sweep_xor(make_params<uint32_t>(c, cb, ce, src, dst, L.stride, rmw, partials, tickets, work, L.ntiles),
+                         L.vw, L.g, grid, sms, s);
         break;
     case Kind::U64:
         launch_sweep_u64(
-            make_params<unsigned long long>(c, cb, ce, src, dst, L.stride, rmw, partials, tickets, L.ntiles), L.vw,
-            L.g, grid, s);
+            make_params<unsigned long long>(c, cb, ce, src, dst, L.stride, rmw, partials, tickets, work, L.ntiles), L.vw,
+            L.g, grid, sms, s);
         break;
     case Kind::F64:
-        launch_sweep_f64(make_params<double>(c, cb, ce, src, dst, L.stride, rmw, partials, tickets, L.ntiles),
-                         L.vw, L.g, grid, s);
+        launch_sweep_f64(make_params<double>(c, cb, ce, src, dst, L.stride, rmw, partials, tickets, work, L.ntiles),
+                         L.vw, L.g, grid, sms, s);
         break;
     case Kind::F32C:
-        launch_sweep_f32c(make_params<float>(c, cb, ce, src, dst, L.stride, rmw, partials, tickets, L.ntiles),
-                          L.vw, L.g, grid, s);
+        launch_sweep_f32c(make_params<float>(c, cb, ce, src, dst, L.stride, rmw, partials, tickets, work, L.ntiles),
+                          L.vw, L.g, grid, sms, s);
         break;
     case Kind::F32:
-        launch_sweep_f32(make_params<float>(c, cb, ce, src, dst, L.stride, rmw, partials, tickets, L.ntiles),
-                         L.vw, L.g, grid, s);
+        launch_sweep_f32(make_params<float>(c, cb, ce, src, dst, L.stride, rmw, partials, tickets, work, L.ntiles),
+                         L.vw, L.g, grid, sms, s);
+        break;
+    case Kind::F64S:
+        launch_sweep_f64s(make_params<DF>(c, cb, ce, src, dst, L.stride, rmw, partials, tickets, work, L.ntiles),
+                          L.vw, L.g, grid, sms, s);
         break;
     }
     return 1;
@@ -259,6 +278,8 @@ DevicePlan* ensure_device_plan(grgx_graph* g) {
     d->num_levels = hp.num_levels;
     d->has_coals = hp.has_coals;
     d->has_miss = hp.has_miss;
+    for (uint32_t x : hp.xtx_new)
+        if (x != COAL_NOT_SET) d->xtx_max = std::max(d->xtx_max, static_cast<double>(x));
     g->dev = std::move(d);
     g->plan.reset();  // the device copy is authoritative; free the host copy
     return g->dev.get();
@@ -321,7 +342,8 @@ void matmul_impl(grgx_graph* g, int dtype, const void* input, uint64_t in_cols, 
     const bool devPtrs = (flags & GRGX_FLAG_DEVICE_POINTERS) != 0;
     const bool overwrite = (flags & GRGX_FLAG_OVERWRITE) != 0;
     const long long K = static_cast<long long>(rows);
-    const Layout L = choose_layout(dtype, K, (flags & GRGX_FLAG_F32_PLAIN) != 0);
+    const Layout L = choose_layout(dtype, K, (flags & GRGX_FLAG_F32_PLAIN) != 0, (flags & GRGX_FLAG_F64_NATIVE) != 0);
+    const bool df = (L.kind == Kind::F64S);
     const size_t esz = io_size(dtype);
     const bool down = (direction == GRGX_DIRECTION_DOWN);
     const bool useMiss = (miss != nullptr) && dp->has_miss;
@@ -366,21 +388,61 @@ void matmul_impl(grgx_graph* g, int dtype, const void* input, uint64_t in_cols, 
                                 : dp->up.n_pieces;
         void* partials = sc.get(static_cast<size_t>(pieces) * L.stride * L.asize);
         const long long nh = down ? (dp->down.n_heavy + dp->seed.n_heavy + dp->miss.n_heavy) : dp->up.n_heavy;
-        unsigned* tickets = static_cast<unsigned*>(sc.get(static_cast<size_t>(nh) * L.ntiles * sizeof(unsigned)));
-        GRGX_CUDA(cudaMemsetAsync(tickets, 0, static_cast<size_t>(nh) * L.ntiles * sizeof(unsigned), s));
+        const long long nslots = down ? (2 + static_cast<long long>(dp->down.lb.size()))
+                                      : static_cast<long long>(dp->up.lb.size());
+        const size_t counterBytes = static_cast<size_t>(nh + nslots) * L.ntiles * sizeof(unsigned);
+        unsigned* tickets = static_cast<unsigned*>(sc.get(counterBytes));
+        GRGX_CUDA(cudaMemsetAsync(tickets, 0, counterBytes, s));
+        unsigned* work = tickets + nh * L.ntiles;  // one set of L.ntiles counters per launch
+
+        // ---- float64 row scales: exponent of each row's largest finite magnitude -------------
+        unsigned long long* rowmax = nullptr;
+        if (df) {
+            rowmax = static_cast<unsigned long long*>(sc.get(static_cast<size_t>(K) * sizeof(unsigned long long)));
+            unsigned long long floor = 0;
+            if (init_kind == GRGX_INIT_XTX) std::memcpy(&floor, &dp->xtx_max, sizeof(floor));
+            launch_fill_u64(rowmax, K, floor, s);
+            launch_rowmax(static_cast<const double*>(dIn), K, in_cols, in_cols, rowmax, s);
+            launches += 2;
+            if (init_kind == GRGX_INIT_VECTOR) launch_rowmax(static_cast<const double*>(dInit), K, 1, 1, rowmax, s);
+            if (init_kind == GRGX_INIT_MATRIX) launch_rowmax(static_cast<const double*>(dInit), K, n, n, rowmax, s);
+            if (down && dMiss) launch_rowmax(static_cast<const double*>(dMiss), K, M, M, rowmax, s);
+            launches += (init_kind == GRGX_INIT_VECTOR || init_kind == GRGX_INIT_MATRIX) + (down && dMiss);
+        }
+        auto load_rows = [&](const void* src, long long ld, long long R, int mode, long long div, const uint32_t* tab,
+                             void* dst, int add) {
+            if (df)
+                launch_load_rows_df(static_cast<const double*>(src), K, ld, R, mode, div, tab, dst, L.stride, add,
+                                    rowmax, s);
+            else
+                launch_load_rows(dtype, src, K, ld, R, mode, div, tab, dst, L.stride, add, s);
+            launches++;
+        };
+        auto store_cols = [&](long long C, int mode, long long fold, const uint32_t* tab, void* out, long long ld,
+                              int add) {
+            if (df)
+                launch_store_cols_df(vals, L.stride, K, C, mode, fold, tab, static_cast<double*>(out), ld, add, rowmax,
+                                     s);
+            else
+                launch_store_cols(dtype, vals, L.stride, K, C, mode, fold, tab, out, ld, add, s);
+            launches++;
+        };
 
         // ---- init -------------------------------------------------------------------------
         switch (init_kind) {
         case GRGX_INIT_VECTOR:
-            launch_init_vector(dtype, dInit, K, n, vals, L.stride, s);
+            if (df)
+                launch_init_vector_df(static_cast<const double*>(dInit), K, n, vals, L.stride, rowmax, s);
+            else
+                launch_init_vector(dtype, dInit, K, n, vals, L.stride, s);
             launches++;
             break;
-        case GRGX_INIT_MATRIX:
-            launch_load_rows(dtype, dInit, K, n, n, MAP_TABLE, 1, dp->new2old, vals, L.stride, 0, s);
-            launches++;
-            break;
+        case GRGX_INIT_MATRIX: load_rows(dInit, n, n, MAP_TABLE, 1, dp->new2old, vals, 0); break;
         case GRGX_INIT_XTX:
-            launch_init_xtx(dtype, dp->xtx_new, K, n, vals, L.stride, s);
+            if (df)
+                launch_init_xtx_df(dp->xtx_new, K, n, vals, L.stride, rowmax, s);
+            else
+                launch_init_xtx(dtype, dp->xtx_new, K, n, vals, L.stride, s);
             launches++;
             break;
         default: GRGX_CUDA(cudaMemsetAsync(vals, 0, valBytes, s)); break;
@@ -392,52 +454,43 @@ void matmul_impl(grgx_graph* g, int dtype, const void* input, uint64_t in_cols, 
             unsigned* tk = tickets;
             if (dp->seed.n_edges > 0) {
                 void* vt = sc.get(static_cast<size_t>(M) * L.stride * L.ssize);
-                launch_load_rows(dtype, dIn, K, in_cols, M, MAP_IDENT, 1, nullptr, vt, L.stride, 0, s);
-                launches++;
-                launches += launch_level(L, dp->seed, 0, vt, vals, hasInit, partials, tk, s);
+                load_rows(dIn, in_cols, M, MAP_IDENT, 1, nullptr, vt, 0);
+                launches += launch_level(L, dp->seed, 0, vt, vals, hasInit, partials, tk, work, s);
             }
             tk += dp->seed.n_heavy * L.ntiles;
             if (useMiss && dp->miss.n_edges > 0) {
                 void* mt = sc.get(static_cast<size_t>(M) * L.stride * L.ssize);
-                launch_load_rows(dtype, dMiss, K, M, M, MAP_IDENT, 1, nullptr, mt, L.stride, 0, s);
-                launches++;
-                launches += launch_level(L, dp->miss, 0, mt, vals, 1, partials, tk, s);
+                load_rows(dMiss, M, M, MAP_IDENT, 1, nullptr, mt, 0);
+                launches += launch_level(L, dp->miss, 0, mt, vals, 1, partials, tk, work + L.ntiles, s);
             }
             tk += dp->miss.n_heavy * L.ntiles;
             if (t_timing) GRGX_CUDA(cudaEventRecord(ev[1], s));
             for (size_t lvl = 0; lvl < dp->down.lb.size(); lvl++)
-                launches += launch_level(L, dp->down, lvl, vals, vals, 1, partials, tk, s);
+                launches += launch_level(L, dp->down, lvl, vals, vals, 1, partials, tk, work + (2 + lvl) * L.ntiles, s);
             if (t_timing) GRGX_CUDA(cudaEventRecord(ev[2], s));
             // ---- gather samples -----------------------------------------------------------------
             const int add = overwrite ? 0 : 1;
             if (emit_all) {
-                launch_store_cols(dtype, vals, L.stride, K, n, MAP_TABLE, 1, dp->old2new, dOut, out_cols, add, s);
+                store_cols(n, MAP_TABLE, 1, dp->old2new, dOut, out_cols, add);
             } else if (by_indiv) {
-                launch_store_cols(dtype, vals, L.stride, K, out_cols, MAP_FOLD, P, nullptr, dOut, out_cols, add, s);
+                store_cols(out_cols, MAP_FOLD, P, nullptr, dOut, out_cols, add);
             } else {
-                launch_store_cols(dtype, vals, L.stride, K, out_cols, MAP_IDENT, 1, nullptr, dOut, out_cols, add, s);
+                store_cols(out_cols, MAP_IDENT, 1, nullptr, dOut, out_cols, add);
             }
-            launches++;
         } else {
             // ---- UP seed: samples <- input columns -------------------------------------------------
-            launch_load_rows(dtype, dIn, K, in_cols, N, by_indiv ? MAP_DIV : MAP_IDENT, P, nullptr, vals, L.stride,
-                             hasInit, s);
-            launches++;
+            load_rows(dIn, in_cols, N, by_indiv ? MAP_DIV : MAP_IDENT, P, nullptr, vals, hasInit);
             if (t_timing) GRGX_CUDA(cudaEventRecord(ev[1], s));
             for (size_t lvl = 0; lvl < dp->up.lb.size(); lvl++)
-                launches += launch_level(L, dp->up, lvl, vals, vals, hasInit, partials, tickets, s);
+                launches += launch_level(L, dp->up, lvl, vals, vals, hasInit, partials, tickets, work + lvl * L.ntiles, s);
             if (t_timing) GRGX_CUDA(cudaEventRecord(ev[2], s));
             const int add = overwrite ? 0 : 1;
             if (emit_all) {
-                launch_store_cols(dtype, vals, L.stride, K, n, MAP_TABLE, 1, dp->old2new, dOut, out_cols, add, s);
+                store_cols(n, MAP_TABLE, 1, dp->old2new, dOut, out_cols, add);
             } else {
-                launch_store_cols(dtype, vals, L.stride, K, M, MAP_TABLE, 1, dp->mut_new, dOut, out_cols, add, s);
-                if (useMiss) {
-                    launch_store_cols(dtype, vals, L.stride, K, M, MAP_TABLE, 1, dp->miss_new, dMiss, M, 1, s);
-                    launches++;
-                }
+                store_cols(M, MAP_TABLE, 1, dp->mut_new, dOut, out_cols, add);
+                if (useMiss) store_cols(M, MAP_TABLE, 1, dp->miss_new, dMiss, M, 1);
             }
-            launches++;
         }
         GRGX_CUDA(cudaGetLastError());
         if (!devPtrs) {

@@ -127,4 +127,91 @@ struct AddF32C {
     }
 };
 
+// Float64 on GB300 without the FP64 pipe in the inner loop.  Node values are stored as a
+// float pair (hi + lo, 48 significant bits) of the value scaled by 2^-e_k per input row k, so
+// each row's largest input sits in [1, 2) and every sum stays well inside float range.  Edge
+// sums run in float-float: TwoSum of the high parts, the rounding error and the low parts
+// folded into lo, then renormalised (the "sloppy" double-word addition; its error is at most a
+// few u^2 (|a| + |b|), u = 2^-24).  Every 32 additions the run is folded into a double, so a
+// run's error is bounded by ~32 * 4u^2 * sum|x| ~ 5e-13 of the terms' magnitudes and the
+// double chain adds the usual 1.1e-16 per fold.  `p` keeps the plain float sum of the high
+// parts, which carries IEEE inf/nan through exactly when an input is not finite.
+struct alignas(8) DF {
+    float hi, lo;
+};
+
+struct F64Run {
+    double acc;
+    float hi, lo, p, pad;
+};
+
+struct AddF64S {
+    using S = DF;
+    using A = F64Run;
+    static __device__ __forceinline__ A zero() { return {0.0, 0.0f, 0.0f, 0.0f, 0.0f}; }
+    static __device__ __forceinline__ void run_add(float& hi, float& lo, float xh, float xl) {
+        const float s = __fadd_rn(hi, xh);
+        const float bb = __fsub_rn(s, hi);
+        float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(xh, bb));
+        e = __fadd_rn(e, __fadd_rn(lo, xl));
+        hi = __fadd_rn(s, e);
+        lo = __fsub_rn(e, __fsub_rn(hi, s));
+    }
+    static __device__ __forceinline__ void add(A& a, S x) {
+        run_add(a.hi, a.lo, x.hi, x.lo);
+        a.p = __fadd_rn(a.p, x.hi);
+    }
+    static __device__ __forceinline__ double run_value(const A& a) {
+        return isfinite(a.p) ? (static_cast<double>(a.hi) + static_cast<double>(a.lo)) : static_cast<double>(a.p);
+    }
+    static __device__ __forceinline__ void flush(A& a) {
+        a.acc += run_value(a);
+        a.hi = a.lo = a.p = 0.0f;
+    }
+    static __device__ __forceinline__ void merge(A& a, const A& b) {
+        a.acc += b.acc;
+        run_add(a.hi, a.lo, b.hi, b.lo);
+        a.p = __fadd_rn(a.p, b.p);
+    }
+    static __device__ __forceinline__ A shfl_xor(const A& a, int m) {
+        A r;
+        r.acc = __shfl_xor_sync(FULL_MASK, a.acc, m);
+        r.hi = __shfl_xor_sync(FULL_MASK, a.hi, m);
+        r.lo = __shfl_xor_sync(FULL_MASK, a.lo, m);
+        r.p = __shfl_xor_sync(FULL_MASK, a.p, m);
+        r.pad = 0.0f;
+        return r;
+    }
+    static __device__ __forceinline__ A shfl_up(const A& a, int d) {
+        A r;
+        r.acc = __shfl_up_sync(FULL_MASK, a.acc, d);
+        r.hi = __shfl_up_sync(FULL_MASK, a.hi, d);
+        r.lo = __shfl_up_sync(FULL_MASK, a.lo, d);
+        r.p = __shfl_up_sync(FULL_MASK, a.p, d);
+        r.pad = 0.0f;
+        return r;
+    }
+    static __device__ __forceinline__ A shfl_down(const A& a, int d) {
+        A r;
+        r.acc = __shfl_down_sync(FULL_MASK, a.acc, d);
+        r.hi = __shfl_down_sync(FULL_MASK, a.hi, d);
+        r.lo = __shfl_down_sync(FULL_MASK, a.lo, d);
+        r.p = __shfl_down_sync(FULL_MASK, a.p, d);
+        r.pad = 0.0f;
+        return r;
+    }
+    static __device__ __forceinline__ S split(double v) {
+        const float hi = __double2float_rn(v);
+        const float lo = isfinite(hi) ? __double2float_rn(v - static_cast<double>(hi)) : 0.0f;
+        return {hi, lo};
+    }
+    static __device__ __forceinline__ double value(S x) {
+        return isfinite(x.hi) ? static_cast<double>(x.hi) + static_cast<double>(x.lo) : static_cast<double>(x.hi);
+    }
+    static __device__ __forceinline__ S finish(const A& a) { return split(a.acc + run_value(a)); }
+    static __device__ __forceinline__ S finish_onto(S base, const A& a) {
+        return split(value(base) + (a.acc + run_value(a)));
+    }
+};
+
 }  // namespace grgx

@@ -43,6 +43,7 @@ template <typename S> struct SweepParams {
     int rmw;                   // add onto the existing dst value
     void* partials;            // Op::A per (slot, column)
     unsigned* tickets;         // per (heavy row, column tile)
+    unsigned* work;            // per column tile: next chunk to take (zeroed before the launch)
     int ntiles;
 };
 
@@ -55,6 +56,8 @@ template <> struct Vec<float, 2> { static __device__ __forceinline__ void ld(con
 template <> struct Vec<float, 4> { static __device__ __forceinline__ void ld(const float* p, float* v) { float4 t = __ldg(reinterpret_cast<const float4*>(p)); v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w; } static __device__ __forceinline__ void st(float* p, const float* v) { *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]); } };
 template <> struct Vec<double, 1> { static __device__ __forceinline__ void ld(const double* p, double* v) { v[0] = __ldg(p); } static __device__ __forceinline__ void st(double* p, const double* v) { p[0] = v[0]; } };
 template <> struct Vec<double, 2> { static __device__ __forceinline__ void ld(const double* p, double* v) { double2 t = __ldg(reinterpret_cast<const double2*>(p)); v[0] = t.x; v[1] = t.y; } static __device__ __forceinline__ void st(double* p, const double* v) { *reinterpret_cast<double2*>(p) = make_double2(v[0], v[1]); } };
+template <> struct Vec<DF, 1> { static __device__ __forceinline__ void ld(const DF* p, DF* v) { float2 t = __ldg(reinterpret_cast<const float2*>(p)); v[0] = {t.x, t.y}; } static __device__ __forceinline__ void st(DF* p, const DF* v) { *reinterpret_cast<float2*>(p) = make_float2(v[0].hi, v[0].lo); } };
+template <> struct Vec<DF, 2> { static __device__ __forceinline__ void ld(const DF* p, DF* v) { float4 t = __ldg(reinterpret_cast<const float4*>(p)); v[0] = {t.x, t.y}; v[1] = {t.z, t.w}; } static __device__ __forceinline__ void st(DF* p, const DF* v) { *reinterpret_cast<float4*>(p) = make_float4(v[0].hi, v[0].lo, v[1].hi, v[1].lo); } };
 template <> struct Vec<unsigned long long, 1> { static __device__ __forceinline__ void ld(const unsigned long long* p, unsigned long long* v) { v[0] = __ldg(p); } static __device__ __forceinline__ void st(unsigned long long* p, const unsigned long long* v) { p[0] = v[0]; } };
 template <> struct Vec<unsigned long long, 2> { static __device__ __forceinline__ void ld(const unsigned long long* p, unsigned long long* v) { ulonglong2 t = __ldg(reinterpret_cast<const ulonglong2*>(p)); v[0] = t.x; v[1] = t.y; } static __device__ __forceinline__ void st(unsigned long long* p, const unsigned long long* v) { *reinterpret_cast<ulonglong2*>(p) = make_ulonglong2(v[0], v[1]); } };
 
@@ -97,25 +100,42 @@ __device__ __forceinline__ uint32_t ld_cg(const uint32_t* p) { return __ldcg(p);
 __device__ __forceinline__ unsigned long long ld_cg(const unsigned long long* p) { return __ldcg(p); }
 __device__ __forceinline__ double ld_cg(const double* p) { return __ldcg(p); }
 __device__ __forceinline__ float ld_cg(const float* p) { return __ldcg(p); }
+__device__ __forceinline__ F64Run ld_cg(const F64Run* p) {
+    // 24-byte records are only 8-byte aligned: three 8-byte loads
+    const double a = __ldcg(reinterpret_cast<const double*>(p));
+    const float2 t = __ldcg(reinterpret_cast<const float2*>(reinterpret_cast<const char*>(p) + 8));
+    const float2 u = __ldcg(reinterpret_cast<const float2*>(reinterpret_cast<const char*>(p) + 16));
+    return {a, t.x, t.y, u.x, u.y};
+}
 __device__ __forceinline__ F32Pair ld_cg(const F32Pair* p) {
     const float2 t = __ldcg(reinterpret_cast<const float2*>(p));
     return {t.x, t.y};
 }
 
+// Accumulation operators may bound the length of their running chains (AddF64S keeps at most
+// 32 additions in its float-float run before folding it into a double); the kernel calls
+// Op::flush after every `flush_steps` steps, where a step gives each lane STEPS additions.
+template <class Op> struct FlushTraits {
+    static constexpr bool kFlush = false;
+    static __device__ __forceinline__ void flush(typename Op::A&) {}
+};
+template <> struct FlushTraits<AddF64S> {
+    static constexpr bool kFlush = true;
+    static __device__ __forceinline__ void flush(F64Run& a) { AddF64S::flush(a); }
+};
+
 template <class Op, int VW, int G>
-__global__ void __launch_bounds__(256) sweep_kernel(const SweepParams<typename Op::S> p) {
+__device__ __forceinline__ void sweep_chunk(const SweepParams<typename Op::S>& p, long long c, int lane) {
     using S = typename Op::S;
     using A = typename Op::A;
-    constexpr int NG = 32 / G;                 // groups per warp = edges per sub-step
-    constexpr int UNR = (G >= 8) ? 1 : 8 / G;  // 32-edge blocks per step
-    constexpr int STEPS = UNR * G;             // sub-steps per step (a multiple of 8)
-    constexpr int BATCH = 8;                   // gathers in flight per lane
+    constexpr int NG = 32 / G;  // groups per warp = edges per sub-step
+    // gathers in flight per lane: 4 for 16-byte vectors, 8 for narrower ones
+    constexpr int BATCH = (VW * sizeof(S) >= 16) ? 4 : 8;
+    constexpr int UNR = (G >= BATCH) ? 1 : BATCH / G;  // 32-edge blocks per step
+    constexpr int STEPS = UNR * G;                     // sub-steps per step (a multiple of BATCH)
     constexpr unsigned NGMASK = (NG == 32) ? 0xffffffffu : ((1u << NG) - 1u);
+    constexpr int FLUSH_EVERY = (STEPS >= 32) ? 1 : 32 / STEPS;
 
-    const int warp = threadIdx.x >> 5;
-    const int lane = threadIdx.x & 31;
-    const long long c = p.c_begin + (long long)blockIdx.x * (blockDim.x >> 5) + warp;
-    if (c >= p.c_end) return;
     const int lg = lane / G;  // group
     const int li = lane % G;  // lane inside the group
     const int col = blockIdx.y * (G * VW) + li * VW;
@@ -130,20 +150,38 @@ __global__ void __launch_bounds__(256) sweep_kernel(const SweepParams<typename O
     for (int i = 0; i < VW; i++) acc[i] = Op::zero();
     long long cur = ch.r0;
     bool first = true;
+    int nsteps = 0;
 
+    uint32_t nraw[UNR];
+#pragma unroll
+    for (int b = 0; b < UNR; b++) {
+        const long long e = ch.e0 + 32 * b + lane;
+        nraw[b] = (e < eEnd) ? __ldg(p.adj + e) : 0u;
+    }
     for (long long base = ch.e0; base < eEnd; base += 32 * UNR) {
         uint32_t raw[UNR];
         unsigned heads[UNR];
+        unsigned anyHead = 0;
 #pragma unroll
         for (int b = 0; b < UNR; b++) {
-            const long long e = base + 32 * b + lane;
-            raw[b] = (e < eEnd) ? __ldg(p.adj + e) : 0u;
+            raw[b] = nraw[b];
             heads[b] = __ballot_sync(FULL_MASK, raw[b] & 0x80000000u);
+            anyHead |= heads[b];
+        }
+        // prefetch the next step's edge ids while this step's gathers are in flight
+        const long long nbase = base + 32 * UNR;
+        if (nbase < eEnd) {
+#pragma unroll
+            for (int b = 0; b < UNR; b++) {
+                const long long e = nbase + 32 * b + lane;
+                nraw[b] = (e < eEnd) ? __ldg(p.adj + e) : 0u;
+            }
         }
         if (first) {
             cur = ch.r0 - (long long)(heads[0] & 1u);
             first = false;
         }
+        const long long left = eEnd - base;  // valid edges from `base`
 #pragma unroll
         for (int t0 = 0; t0 < STEPS; t0 += BATCH) {
             S v[BATCH][VW];
@@ -153,12 +191,21 @@ __global__ void __launch_bounds__(256) sweep_kernel(const SweepParams<typename O
                 const int b = t / G, s = t % G;
                 const int j = s * NG + lg;
                 const uint32_t idx = __shfl_sync(FULL_MASK, raw[b], j) & 0x7fffffffu;
-                if (base + 32 * b + j < eEnd && colok) {
+                if (32 * b + j < left && colok) {
                     Vec<S, VW>::ld(p.src + (long long)idx * p.stride + col, v[u]);
                 } else {
 #pragma unroll
-                    for (int i = 0; i < VW; i++) v[u][i] = S(0);
+                    for (int i = 0; i < VW; i++) v[u][i] = S{};
                 }
+            }
+            if (anyHead == 0u) {
+                // no row starts in this step: every edge continues the current row
+#pragma unroll
+                for (int u = 0; u < BATCH; u++) {
+#pragma unroll
+                    for (int i = 0; i < VW; i++) Op::add(acc[i], v[u][i]);
+                }
+                continue;
             }
 #pragma unroll
             for (int u = 0; u < BATCH; u++) {
@@ -211,6 +258,13 @@ __global__ void __launch_bounds__(256) sweep_kernel(const SweepParams<typename O
                 cur += Q;
             }
         }
+        if constexpr (FlushTraits<Op>::kFlush) {
+            if (++nsteps == FLUSH_EVERY) {
+                nsteps = 0;
+#pragma unroll
+                for (int i = 0; i < VW; i++) FlushTraits<Op>::flush(acc[i]);
+            }
+        }
     }
 
     group_allreduce<Op, VW, G>(acc);
@@ -245,6 +299,26 @@ __global__ void __launch_bounds__(256) sweep_kernel(const SweepParams<typename O
     }
     group_allreduce<Op, VW, G>(sum);
     if (lg == 0 && colok) write_row<Op, VW>(p, cur, col, sum);
+}
+
+// Persistent warps: each warp takes chunks of the level from a shared counter until none are
+// left, so long and short chunks balance across the SMs.
+// Blocks per SM the register budget is sized for (65536 / (256 * blocks) registers per thread).
+template <class Op, int VW, int G> struct SweepOccupancy {
+    static constexpr int kBlocks = 4;
+};
+
+template <class Op, int VW, int G>
+__global__ void __launch_bounds__(256, SweepOccupancy<Op, VW, G>::kBlocks) sweep_kernel(const SweepParams<typename Op::S> p) {
+    const int lane = threadIdx.x & 31;
+    unsigned* counter = p.work + blockIdx.y;
+    for (;;) {
+        long long c = 0;
+        if (lane == 0) c = (long long)atomicAdd(counter, 1u);
+        c = __shfl_sync(FULL_MASK, c, 0) + p.c_begin;
+        if (c >= p.c_end) return;
+        sweep_chunk<Op, VW, G>(p, c, lane);
+    }
 }
 
 }  // namespace grgx

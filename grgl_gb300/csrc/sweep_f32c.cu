@@ -2,7 +2,7 @@
 #include "sweep_inst.cuh"
 
 namespace grgx {
-void launch_sweep_f32c(const SweepParams<float>& p, int vw, int g, dim3 grid, cudaStream_t s) {
+void launch_sweep_f32c(const SweepParams<float>& p, int vw, int g, dim3 grid, int sms, cudaStream_t s) {
     GRGX_SWEEP_DISPATCH4(AddF32C)
 }
 }  // namespace grgx

@@ -4,8 +4,17 @@
 
 #include "launch.h"
 
+// Persistent grid: at most as many blocks as can be resident at once.
 #define GRGX_SWEEP_CASE(OP, VWV, GV)                                                  \
     if (vw == VWV && g == GV) {                                                       \
+        static int perSm = 0;                                                         \
+        if (perSm == 0) {                                                             \
+            int nb = 0;                                                               \
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, sweep_kernel<OP, VWV, GV>, 256, 0); \
+            perSm = nb > 0 ? nb : 1;                                                  \
+        }                                                                             \
+        const unsigned cap = (unsigned)(perSm * sms);                                 \
+        if (grid.x > cap) grid.x = cap;                                               \
         sweep_kernel<OP, VWV, GV><<<grid, 256, 0, s>>>(p);                            \
         return;                                                                       \
     }

@@ -60,6 +60,7 @@ typedef enum { GRGX_INIT_ZERO = 0, GRGX_INIT_VECTOR = 1, GRGX_INIT_MATRIX = 2, G
 #define GRGX_FLAG_F32_PLAIN 0x2u       /* f32: plain (uncompensated) accumulation */
 #define GRGX_FLAG_SYNC 0x4u            /* wait for the stream before returning */
 #define GRGX_FLAG_OVERWRITE 0x8u       /* write the output instead of adding to it */
+#define GRGX_FLAG_F64_NATIVE 0x10u     /* f64: accumulate on the FP64 pipe instead of as scaled float pairs */
 
 typedef struct {
     uint64_t num_nodes;

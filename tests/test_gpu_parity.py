@@ -217,3 +217,40 @@ def test_large_window_tree_properties(gx):
     assert np.array_equal(gx.matmul(g, 3 * a - 7 * b, UP), 3 * gx.matmul(g, a, UP) - 7 * gx.matmul(g, b, UP))
     # DOWN(1) per sample is the number of mutations carried; UP(1) per mutation its count
     assert up.min() >= 1 and down.max() <= M
+
+
+def test_f64_extreme_magnitudes_and_native(gx, wt):
+    """float64 rows are scaled by powers of two before the float-pair sweep: rows of 1e300,
+    1e-300 and mixed magnitudes keep 1e-12 accuracy; the FP64-pipe variant agrees too."""
+    g, og = wt
+    rng = np.random.default_rng(12)
+    for direction, cols in ((UP, og.num_samples), (DOWN, og.num_mutations)):
+        V = rng.standard_normal((4, cols))
+        V[0] *= 1e300
+        V[1] *= 1e-300
+        V[2, ::7] *= 1e200
+        V[3] *= 1e-310  # subnormal row
+        ref = oracle.matmul(og, V, direction)
+        scale = oracle.matmul(og, np.abs(V), direction)
+        assert_matches(gx.matmul(g, V, direction), ref, scale)
+        assert_matches(gx.matmul(g, V, direction, f64_native=True), ref, scale)
+
+
+def test_f64_nonfinite_propagates_like_reference(gx, wt):
+    g, og = wt
+    rng = np.random.default_rng(13)
+    for direction, cols in ((UP, og.num_samples), (DOWN, og.num_mutations)):
+        V = rng.standard_normal((3, cols))
+        V[0, 5] = np.inf
+        V[1, 9] = np.nan
+        V[2, 3], V[2, 4] = np.inf, -np.inf
+        with np.errstate(invalid="ignore"):
+            ref = oracle.matmul(og, V, direction)
+            got = gx.matmul(g, V, direction)
+        assert np.array_equal(np.isnan(got), np.isnan(ref))
+        assert np.array_equal(np.isposinf(got), np.isposinf(ref))
+        assert np.array_equal(np.isneginf(got), np.isneginf(ref))
+        fin = np.isfinite(ref)
+        with np.errstate(invalid="ignore"):
+            scale = oracle.matmul(og, np.where(np.isfinite(V), np.abs(V), 0.0), direction)
+        assert np.all(np.abs(got[fin] - ref[fin]) <= 1e-12 * scale[fin] + 1e-300)
