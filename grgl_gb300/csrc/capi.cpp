@@ -197,6 +197,12 @@ grgx_status grgx_matmul(grgx_graph* g, grgx_dtype dtype, const void* input, uint
 
 void grgx_set_timing(int enabled) { set_timing(enabled); }
 
+// Host-only helper for profiling the plan build (not part of the public header).
+double grgx_plan_benchmark(grgx_graph* g) {
+    auto p = build_plan(*g->host);
+    return static_cast<double>(p->up.adj.size());
+}
+
 grgx_status grgx_last_timing(grgx_timing* out) {
     return guarded([&] {
         GRGX_CHECK(out, GRGX_ERR_API_MISUSE, "null argument");

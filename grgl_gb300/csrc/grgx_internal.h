@@ -78,7 +78,10 @@ static_assert(sizeof(HeavyRow) == 16, "HeavyRow layout");
 // A pull-form CSR over (renumbered) node ids, arranged level by level in processing order.
 struct PullCSR {
     std::vector<int32_t> rows;     // row -> destination node id
-    std::vector<uint32_t> adj;     // source ids, HEAD_BIT on each row's first edge
+    std::vector<uint32_t> adj;     // source ids, HEAD_BIT on each row's first edge (empty when
+                                   // the adjacency is built on the device, see HostPlan::down)
+    std::vector<int64_t> off;      // row offsets (kept for device-side construction)
+    int64_t num_edges = 0;
     std::vector<Chunk> chunks;     // + sentinel {E, R, -1}
     std::vector<HeavyRow> heavy;
     std::vector<int32_t> level_chunk_begin;  // per processed level, chunk range [b, e)
@@ -93,6 +96,8 @@ struct HostPlan {
     std::vector<uint64_t> level_begin;    // new-id range of each height
     PullCSR up;     // levels 1..H ascending; rows = nodes, adj = children
     PullCSR down;   // levels H..0 descending; rows = nodes with parents, adj = parents
+                    // (adj left empty: built on the device from `up` by a stable sort)
+    std::vector<int32_t> down_row_of;  // new id -> DOWN row (or -1)
     PullCSR seed;   // one "level": rows = mutation nodes, adj = mutation ids
     PullCSR miss;   // one "level": rows = missingness nodes, adj = mutation ids
     std::vector<uint32_t> mut_new, miss_new;  // mutation -> new node id (or INVALID)

@@ -82,7 +82,7 @@ template <typename T> T* upload(DevicePlan& d, const std::vector<T>& v) {
 
 DevCSR upload_csr(DevicePlan& d, const PullCSR& c) {
     DevCSR r;
-    r.adj = upload(d, c.adj);
+    r.adj = upload(d, c.adj);  // null when the adjacency is built on the device
     r.rows = upload(d, c.rows);
     r.chunks = reinterpret_cast<ChunkDev*>(upload(d, c.chunks));
     r.heavy = reinterpret_cast<HeavyDev*>(upload(d, c.heavy));
@@ -90,7 +90,7 @@ DevCSR upload_csr(DevicePlan& d, const PullCSR& c) {
     r.le = c.level_chunk_end;
     r.n_heavy = static_cast<long long>(c.heavy.size());
     r.n_pieces = c.num_pieces;
-    r.n_edges = static_cast<long long>(c.adj.size());
+    r.n_edges = c.num_edges;
     r.n_rows = static_cast<long long>(c.rows.size());
     return r;
 }
@@ -252,6 +252,9 @@ size_t io_size(int dtype) {
 
 }  // namespace
 
+uint32_t* build_down_adj_device(const uint32_t* upAdj, const int* upRows, const ChunkDev* upChunks, long long upChunkCount,
+                                long long E, const std::vector<int32_t>& rowOf, const std::vector<int64_t>& downOff);
+
 DevicePlan* ensure_device_plan(grgx_graph* g) {
     std::lock_guard<std::mutex> lk(g->mu);
     int device = 0;
@@ -268,6 +271,13 @@ DevicePlan* ensure_device_plan(grgx_graph* g) {
     d->device = device;
     d->up = upload_csr(*d, hp.up);
     d->down = upload_csr(*d, hp.down);
+    d->down.adj = build_down_adj_device(d->up.adj, d->up.rows, d->up.chunks,
+                                        static_cast<long long>(hp.up.chunks.size()) - 1, hp.down.num_edges,
+                                        hp.down_row_of, hp.down.off);
+    if (d->down.adj) {
+        d->allocs.push_back(d->down.adj);
+        d->bytes += static_cast<uint64_t>(hp.down.num_edges) * sizeof(uint32_t);
+    }
     d->seed = upload_csr(*d, hp.seed);
     d->miss = upload_csr(*d, hp.miss);
     d->mut_new = upload(*d, hp.mut_new);

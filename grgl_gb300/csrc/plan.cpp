@@ -15,6 +15,9 @@
 // edges than the chunk size is cut into pieces whose partial sums are combined in piece order.
 #include <algorithm>
 #include <atomic>
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
 #include <functional>
 #include <numeric>
 #include <thread>
@@ -88,6 +91,7 @@ void chunk_level(PullCSR& P, const std::vector<int64_t>& off, int64_t rb, int64_
 
 void finish_csr(PullCSR& P, const std::vector<int64_t>& off) {
     P.chunks.push_back(Chunk{off.back(), static_cast<int32_t>(P.rows.size()), -1});
+    P.num_edges = off.back();
     GRGX_CHECK(P.chunks.size() < 0x7fffffffull && P.heavy.size() < 0x7fffffffull, GRGX_ERR_UNSUPPORTED,
                "graph too large for the chunk index");
 }
@@ -112,7 +116,22 @@ void single_level_csr(PullCSR& P, const std::vector<std::pair<uint32_t, uint32_t
 
 }  // namespace
 
+namespace {
+struct PhaseTimer {
+    const char* name;
+    std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+    bool on = std::getenv("GRGX_PLAN_TIMING") != nullptr;
+    void lap(const char* what) {
+        if (!on) return;
+        const auto t1 = std::chrono::steady_clock::now();
+        std::fprintf(stderr, "[plan] %-12s %8.3f s\n", what, std::chrono::duration<double>(t1 - t0).count());
+        t0 = t1;
+    }
+};
+}  // namespace
+
 std::unique_ptr<HostPlan> build_plan(const HostGraph& g) {
+    PhaseTimer timer{"plan"};
     const uint64_t n = g.num_nodes, N = g.num_samples;
     GRGX_CHECK(n <= MAX_NODES, GRGX_ERR_UNSUPPORTED, "too many nodes");
     auto plan = std::make_unique<HostPlan>();
@@ -159,6 +178,7 @@ std::unique_ptr<HostPlan> build_plan(const HostGraph& g) {
             height[v] = h;
         }
     }
+    timer.lap("heights");
     for (uint64_t s = 0; s < N; s++)
         GRGX_CHECK(height[s] == 0, GRGX_ERR_UNSUPPORTED, "sample nodes with children are not supported");
     uint32_t maxH = 0;
@@ -183,6 +203,7 @@ std::unique_ptr<HostPlan> build_plan(const HostGraph& g) {
     const auto& o2n = plan->old2new;
     const auto& n2o = plan->new2old;
 
+    timer.lap("renumber");
     // ---- UP: rows = every node of heights 1..H, children in stored order --------------------
     {
         PullCSR& P = plan->up;
@@ -208,13 +229,48 @@ std::unique_ptr<HostPlan> build_plan(const HostGraph& g) {
             chunk_level(P, off, static_cast<int64_t>(plan->level_begin[h] - r0),
                         static_cast<int64_t>(plan->level_begin[h + 1] - r0));
         finish_csr(P, off);
+        P.off = std::move(off);
     }
 
+    timer.lap("up csr");
     // ---- DOWN: rows = nodes with parents, heights H..0, parents ascending by new id ---------
+    // The host counts parents per node (parallel, per-thread counters) to lay out rows, offsets
+    // and chunks; the adjacency itself is built on the device from the UP CSR (plan_gpu.cu).
     {
         PullCSR& P = plan->down;
-        std::vector<uint64_t> pdeg(n + 1, 0);  // parent counts by new id
-        for (uint64_t e = 0; e < g.num_edges(); e++) pdeg[o2n[g.down_adj[e]]]++;
+        const int T = (g.num_edges() < (1u << 20)) ? 1 : host_threads();
+        // parent ranges balanced by edge count
+        std::vector<uint64_t> pb(T + 1, 0);
+        {
+            std::vector<uint64_t> cum(n + 1, 0);
+            for (uint64_t pid = 0; pid < n; pid++) {
+                const uint32_t old = n2o[pid];
+                cum[pid + 1] = cum[pid] + (g.down_off[old + 1] - g.down_off[old]);
+            }
+            for (int t = 1; t < T; t++)
+                pb[t] = static_cast<uint64_t>(std::lower_bound(cum.begin(), cum.end(), cum[n] * t / T) - cum.begin());
+            pb[T] = n;
+        }
+        timer.lap("down.ranges");
+        std::vector<std::vector<uint32_t>> cnt(T, std::vector<uint32_t>(n, 0));
+        parallel_for(T, [&](uint64_t b, uint64_t e, int) {
+            for (uint64_t t = b; t < e; t++) {
+                std::vector<uint32_t>& c = cnt[t];
+                for (uint64_t pid = pb[t]; pid < pb[t + 1]; pid++) {
+                    const uint32_t old = n2o[pid];
+                    for (uint64_t x = g.down_off[old]; x < g.down_off[old + 1]; x++) c[o2n[g.down_adj[x]]]++;
+                }
+            }
+        }, T);
+        timer.lap("down.count");
+        std::vector<uint64_t> pdeg(n, 0);
+        parallel_for(n, [&](uint64_t b, uint64_t e, int) {
+            for (uint64_t c = b; c < e; c++) {
+                uint64_t d = 0;
+                for (int t = 0; t < T; t++) d += cnt[t][c];
+                pdeg[c] = d;
+            }
+        });
         // Row order: heights descending, ids ascending inside a height.
         std::vector<uint32_t> rowNode;
         rowNode.reserve(n);
@@ -224,24 +280,12 @@ std::unique_ptr<HostPlan> build_plan(const HostGraph& g) {
                 if (pdeg[id]) rowNode.push_back(static_cast<uint32_t>(id));
         }
         const uint64_t R = rowNode.size();
-        std::vector<int64_t> rowOf(n, -1);
         std::vector<int64_t> off(R + 1, 0);
-        for (uint64_t i = 0; i < R; i++) {
-            rowOf[rowNode[i]] = static_cast<int64_t>(i);
-            off[i + 1] = off[i] + static_cast<int64_t>(pdeg[rowNode[i]]);
-        }
+        for (uint64_t i = 0; i < R; i++) off[i + 1] = off[i] + static_cast<int64_t>(pdeg[rowNode[i]]);
         P.rows.assign(rowNode.begin(), rowNode.end());
-        P.adj.resize(off[R]);
-        // Fill parents in ascending new id: walk parents by new id.
-        std::vector<int64_t> cursor(off.begin(), off.end() - 1);
-        for (uint64_t pid = 0; pid < n; pid++) {
-            const uint32_t old = n2o[pid];
-            for (uint64_t x = g.down_off[old]; x < g.down_off[old + 1]; x++) {
-                const int64_t row = rowOf[o2n[g.down_adj[x]]];
-                P.adj[cursor[row]++] = static_cast<uint32_t>(pid);
-            }
-        }
-        for (uint64_t i = 0; i < R; i++) P.adj[off[i]] |= HEAD_BIT;
+        plan->down_row_of.assign(n, -1);
+        for (uint64_t i = 0; i < R; i++) plan->down_row_of[rowNode[i]] = static_cast<int32_t>(i);
+        timer.lap("down.rows");
         // Level ranges over rows.
         uint64_t rb = 0;
         for (uint64_t hh = L; hh > 0; hh--) {
@@ -252,8 +296,10 @@ std::unique_ptr<HostPlan> build_plan(const HostGraph& g) {
             rb = re;
         }
         finish_csr(P, off);
+        P.off = std::move(off);
     }
 
+    timer.lap("down csr");
     // ---- mutation seeds / gathers -----------------------------------------------------------
     plan->mut_new.assign(g.num_mutations, INVALID_NODE);
     std::vector<std::pair<uint32_t, uint32_t>> pairs;
@@ -296,6 +342,7 @@ std::unique_ptr<HostPlan> build_plan(const HostGraph& g) {
             plan->xtx_new[id] = c * 2u;
         }
     }
+    timer.lap("seeds/xtx");
     return plan;
 }
 
