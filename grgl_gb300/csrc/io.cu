@@ -63,8 +63,10 @@ template <typename S> __device__ __forceinline__ S s_add(S a, S b) { return a + 
 template <typename IO>
 __global__ void load_rows_kernel(const IO* __restrict__ src, long long K, long long ld, long long R, int mode,
                                  long long div, const uint32_t* __restrict__ tab,
-                                 typename Store<IO>::S* __restrict__ dst, long long stride, int add) {
+                                 typename Store<IO>::S* __restrict__ dst, long long stride, int add,
+                                 const int* gate, int gate_value) {
     using S = typename Store<IO>::S;
+    if (gate != nullptr && *gate != gate_value) return;
     __shared__ S tile[32][33];
     const long long i0 = (long long)blockIdx.x * 32, k0 = (long long)blockIdx.y * 32;
     const int tx = threadIdx.x, ty = threadIdx.y;
@@ -94,8 +96,9 @@ __global__ void load_rows_kernel(const IO* __restrict__ src, long long K, long l
 template <typename IO>
 __global__ void store_cols_kernel(const typename Store<IO>::S* __restrict__ vals, long long stride, long long K,
                                   long long C, int mode, long long fold, const uint32_t* __restrict__ tab,
-                                  IO* __restrict__ out, long long ld, int add) {
+                                  IO* __restrict__ out, long long ld, int add, const int* gate, int gate_value) {
     using S = typename Store<IO>::S;
+    if (gate != nullptr && *gate != gate_value) return;
     __shared__ S tile[32][33];
     const long long c0 = (long long)blockIdx.x * 32, k0 = (long long)blockIdx.y * 32;
     const int tx = threadIdx.x, ty = threadIdx.y;
@@ -128,8 +131,10 @@ __global__ void store_cols_kernel(const typename Store<IO>::S* __restrict__ vals
 
 template <typename IO>
 __global__ void init_vector_kernel(const IO* __restrict__ init, long long K, long long n,
-                                   typename Store<IO>::S* __restrict__ vals, long long stride) {
+                                   typename Store<IO>::S* __restrict__ vals, long long stride, const int* gate,
+                                   int gate_value) {
     using S = typename Store<IO>::S;
+    if (gate != nullptr && *gate != gate_value) return;
     const long long total = n * stride;
     for (long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x; x < total;
          x += (long long)gridDim.x * blockDim.x) {
@@ -140,8 +145,10 @@ __global__ void init_vector_kernel(const IO* __restrict__ init, long long K, lon
 
 template <typename IO>
 __global__ void init_xtx_kernel(const uint32_t* __restrict__ xtx, long long K, long long n,
-                                typename Store<IO>::S* __restrict__ vals, long long stride) {
+                                typename Store<IO>::S* __restrict__ vals, long long stride, const int* gate,
+                                int gate_value) {
     using S = typename Store<IO>::S;
+    if (gate != nullptr && *gate != gate_value) return;
     const long long total = n * stride;
     for (long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x; x < total;
          x += (long long)gridDim.x * blockDim.x) {
@@ -190,20 +197,20 @@ __global__ void store_bits_kernel(const uint32_t* __restrict__ vals, long long s
 
 template <typename IO>
 void load_rows_t(const void* src, long long K, long long ld, long long R, int mode, long long div, const uint32_t* tab,
-                 void* dst, long long stride, int add, cudaStream_t s) {
+                 void* dst, long long stride, int add, const int* gate, int gv, cudaStream_t s) {
     if (R <= 0) return;
     const dim3 grid((unsigned)((R + 31) / 32), (unsigned)((stride + 31) / 32));
     load_rows_kernel<IO><<<grid, dim3(32, 8), 0, s>>>(static_cast<const IO*>(src), K, ld, R, mode, div, tab,
-                                                      static_cast<typename Store<IO>::S*>(dst), stride, add);
+                                                      static_cast<typename Store<IO>::S*>(dst), stride, add, gate, gv);
 }
 
 template <typename IO>
 void store_cols_t(const void* vals, long long stride, long long K, long long C, int mode, long long fold,
-                  const uint32_t* tab, void* out, long long ld, int add, cudaStream_t s) {
+                  const uint32_t* tab, void* out, long long ld, int add, const int* gate, int gv, cudaStream_t s) {
     if (C <= 0 || K <= 0) return;
     const dim3 grid((unsigned)((C + 31) / 32), (unsigned)((K + 31) / 32));
     store_cols_kernel<IO><<<grid, dim3(32, 8), 0, s>>>(static_cast<const typename Store<IO>::S*>(vals), stride, K,
-                                                       C, mode, fold, tab, static_cast<IO*>(out), ld, add);
+                                                       C, mode, fold, tab, static_cast<IO*>(out), ld, add, gate, gv);
 }
 
 unsigned grid_for(long long total) {
@@ -230,7 +237,8 @@ unsigned grid_for(long long total) {
     }
 
 void launch_load_rows(int dtype, const void* src, long long K, long long ld, long long R, int mode, long long div,
-                      const uint32_t* tab, void* dst, long long stride, int add, cudaStream_t s) {
+                      const uint32_t* tab, void* dst, long long stride, int add, cudaStream_t s, const int* gate,
+                      int gv) {
     if (dtype == GRGX_BOOL) {
         if (R <= 0) return;
         const dim3 grid((unsigned)((R + 127) / 128), (unsigned)stride);
@@ -238,13 +246,14 @@ void launch_load_rows(int dtype, const void* src, long long K, long long ld, lon
                                               static_cast<uint32_t*>(dst), stride, add);
         return;
     }
-#define CALL(T) load_rows_t<T>(src, K, ld, R, mode, div, tab, dst, stride, add, s)
+#define CALL(T) load_rows_t<T>(src, K, ld, R, mode, div, tab, dst, stride, add, gate, gv, s)
     GRGX_IO_DISPATCH(dtype, CALL)
 #undef CALL
 }
 
 void launch_store_cols(int dtype, const void* vals, long long stride, long long K, long long C, int mode,
-                       long long fold, const uint32_t* tab, void* out, long long ld, int add, cudaStream_t s) {
+                       long long fold, const uint32_t* tab, void* out, long long ld, int add, cudaStream_t s,
+                       const int* gate, int gv) {
     if (dtype == GRGX_BOOL) {
         if (C <= 0 || K <= 0) return;
         const dim3 grid((unsigned)((C + 127) / 128), (unsigned)K);
@@ -252,26 +261,26 @@ void launch_store_cols(int dtype, const void* vals, long long stride, long long 
                                                static_cast<uint8_t*>(out), ld, add);
         return;
     }
-#define CALL(T) store_cols_t<T>(vals, stride, K, C, mode, fold, tab, out, ld, add, s)
+#define CALL(T) store_cols_t<T>(vals, stride, K, C, mode, fold, tab, out, ld, add, gate, gv, s)
     GRGX_IO_DISPATCH(dtype, CALL)
 #undef CALL
 }
 
 void launch_init_vector(int dtype, const void* init, long long K, long long n, void* vals, long long stride,
-                        cudaStream_t s) {
+                        cudaStream_t s, const int* gate, int gv) {
     const unsigned grid = grid_for(n * stride);
 #define CALL(T)                                                                                            \
     init_vector_kernel<T><<<grid, 256, 0, s>>>(static_cast<const T*>(init), K, n,                          \
-                                               static_cast<typename Store<T>::S*>(vals), stride)
+                                               static_cast<typename Store<T>::S*>(vals), stride, gate, gv)
     GRGX_IO_DISPATCH(dtype, CALL)
 #undef CALL
 }
 
 void launch_init_xtx(int dtype, const uint32_t* xtx, long long K, long long n, void* vals, long long stride,
-                     cudaStream_t s) {
+                     cudaStream_t s, const int* gate, int gv) {
     const unsigned grid = grid_for(n * stride);
 #define CALL(T) \
-    init_xtx_kernel<T><<<grid, 256, 0, s>>>(xtx, K, n, static_cast<typename Store<T>::S*>(vals), stride)
+    init_xtx_kernel<T><<<grid, 256, 0, s>>>(xtx, K, n, static_cast<typename Store<T>::S*>(vals), stride, gate, gv)
     GRGX_IO_DISPATCH(dtype, CALL)
 #undef CALL
 }

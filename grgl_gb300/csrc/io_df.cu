@@ -14,12 +14,18 @@ namespace {
 constexpr uint32_t kInvalid = 0x7fffffffu;
 constexpr unsigned long long kExpMask = 0x7ff0000000000000ull;
 
+// Scale exponent of row k: the row is multiplied by 2^-row_exp, which puts its largest value in
+// [2^60, 2^61) (clamped so both 2^row_exp and 2^-row_exp are normal doubles).
 __device__ __forceinline__ int row_exp(const unsigned long long* rowmax, long long k) {
     const unsigned long long b = rowmax[k];
     if (b == 0) return 0;
-    int e = static_cast<int>((b >> 52) & 0x7ff) - 1023;
+    int e = static_cast<int>((b >> 52) & 0x7ff) - 1023 - 60;
     return e < -1022 ? -1022 : (e > 1022 ? 1022 : e);
 }
+
+// Binades spanned by the nonzero finite magnitudes of a row beyond which the float-pair path
+// would lose the smallest terms (max at 2^60, float normals reach 2^-126).
+constexpr int kMaxBinades = 180;
 
 // 2^e for e in [-1022, 1023], built from its bit pattern (exact).
 __device__ __forceinline__ double pow2(int e) {
@@ -32,36 +38,67 @@ __global__ void fill_u64_kernel(unsigned long long* p, long long n, unsigned lon
 }
 
 __global__ void rowmax_kernel(const double* __restrict__ src, long long K, long long ld, long long cols,
-                              unsigned long long* __restrict__ rowmax) {
-    __shared__ unsigned long long red[8];
+                              unsigned long long* __restrict__ rowmax, unsigned long long* __restrict__ rowmin) {
+    __shared__ unsigned long long redMax[8], redMin[8];
     for (long long k = blockIdx.y; k < K; k += gridDim.y) {
-        unsigned long long m = 0;
+        unsigned long long m = 0, mn = ~0ull;
         for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < cols;
              c += (long long)gridDim.x * blockDim.x) {
             const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(src[k * ld + c])) &
                                          0x7fffffffffffffffull;
-            if ((b & kExpMask) != kExpMask && b > m) m = b;  // finite only
+            if ((b & kExpMask) != kExpMask) {  // finite only
+                m = b > m ? b : m;
+                if (b != 0) mn = b < mn ? b : mn;
+            }
         }
         for (int o = 16; o > 0; o >>= 1) {
             const unsigned long long t = __shfl_xor_sync(0xffffffffu, m, o);
+            const unsigned long long u = __shfl_xor_sync(0xffffffffu, mn, o);
             m = t > m ? t : m;
+            mn = u < mn ? u : mn;
         }
-        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+        if ((threadIdx.x & 31) == 0) {
+            redMax[threadIdx.x >> 5] = m;
+            redMin[threadIdx.x >> 5] = mn;
+        }
         __syncthreads();
         if (threadIdx.x == 0) {
-            unsigned long long r = 0;
-            for (int w = 0; w < (int)(blockDim.x >> 5); w++) r = red[w] > r ? red[w] : r;
+            unsigned long long r = 0, q = ~0ull;
+            for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
+                r = redMax[w] > r ? redMax[w] : r;
+                q = redMin[w] < q ? redMin[w] : q;
+            }
             if (r) atomicMax(rowmax + k, r);
+            if (q != ~0ull) atomicMin(rowmin + k, q);
         }
         __syncthreads();
     }
+}
+
+__global__ void decide_kernel(const unsigned long long* __restrict__ rowmax, const unsigned long long* __restrict__ rowmin,
+                              long long K, int* __restrict__ gate) {
+    __shared__ int wide;
+    if (threadIdx.x == 0) wide = 0;
+    __syncthreads();
+    for (long long k = threadIdx.x; k < K; k += blockDim.x) {
+        const unsigned long long mx = rowmax[k], mn = rowmin[k];
+        if (mx == 0 || mn == ~0ull) continue;
+        const int emax = static_cast<int>((mx >> 52) & 0x7ff), emin = static_cast<int>((mn >> 52) & 0x7ff);
+        const int re = row_exp(rowmax, k);
+        // subnormal terms, or scaled magnitudes outside [2^-120, 2^62]
+        if (emin == 0 || emax - emin > kMaxBinades || (emin - 1023) - re < -120 || (emax - 1023) - re > 62) wide = 1;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) gate[0] = wide;
 }
 
 __device__ __forceinline__ DF split_scaled(double x, int e) { return AddF64S::split(x * pow2(-e)); }
 
 __global__ void load_rows_df_kernel(const double* __restrict__ src, long long K, long long ld, long long R, int mode,
                                     long long div, const uint32_t* __restrict__ tab, DF* __restrict__ dst,
-                                    long long stride, int add, const unsigned long long* __restrict__ rowmax) {
+                                    long long stride, int add, const unsigned long long* __restrict__ rowmax,
+                                    const int* gate) {
+    if (gate != nullptr && *gate != 0) return;
     __shared__ DF tile[32][33];
     const long long i0 = (long long)blockIdx.x * 32, k0 = (long long)blockIdx.y * 32;
     const int tx = threadIdx.x, ty = threadIdx.y;
@@ -91,7 +128,8 @@ __global__ void load_rows_df_kernel(const double* __restrict__ src, long long K,
 __global__ void store_cols_df_kernel(const DF* __restrict__ vals, long long stride, long long K, long long C,
                                      int mode, long long fold, const uint32_t* __restrict__ tab,
                                      double* __restrict__ out, long long ld, int add,
-                                     const unsigned long long* __restrict__ rowmax) {
+                                     const unsigned long long* __restrict__ rowmax, const int* gate) {
+    if (gate != nullptr && *gate != 0) return;
     __shared__ double tile[32][33];
     const long long c0 = (long long)blockIdx.x * 32, k0 = (long long)blockIdx.y * 32;
     const int tx = threadIdx.x, ty = threadIdx.y;
@@ -122,7 +160,9 @@ __global__ void store_cols_df_kernel(const DF* __restrict__ vals, long long stri
 }
 
 __global__ void init_vector_df_kernel(const double* __restrict__ init, long long K, long long n, DF* __restrict__ vals,
-                                      long long stride, const unsigned long long* __restrict__ rowmax) {
+                                      long long stride, const unsigned long long* __restrict__ rowmax,
+                                      const int* gate) {
+    if (gate != nullptr && *gate != 0) return;
     const long long total = n * stride;
     for (long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x; x < total;
          x += (long long)gridDim.x * blockDim.x) {
@@ -132,7 +172,8 @@ __global__ void init_vector_df_kernel(const double* __restrict__ init, long long
 }
 
 __global__ void init_xtx_df_kernel(const uint32_t* __restrict__ xtx, long long K, long long n, DF* __restrict__ vals,
-                                   long long stride, const unsigned long long* __restrict__ rowmax) {
+                                   long long stride, const unsigned long long* __restrict__ rowmax, const int* gate) {
+    if (gate != nullptr && *gate != 0) return;
     const long long total = n * stride;
     for (long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x; x < total;
          x += (long long)gridDim.x * blockDim.x) {
@@ -155,40 +196,46 @@ void launch_fill_u64(unsigned long long* p, long long n, unsigned long long v, c
 }
 
 void launch_rowmax(const double* src, long long K, long long ld, long long cols, unsigned long long* rowmax,
-                   cudaStream_t s) {
+                   unsigned long long* rowmin, cudaStream_t s) {
     if (K <= 0 || cols <= 0) return;
     long long bx = (cols + 256 * 8 - 1) / (256 * 8);
     if (bx > 1024) bx = 1024;
     const long long by = K < 65535 ? K : 65535;
-    rowmax_kernel<<<dim3((unsigned)bx, (unsigned)by), 256, 0, s>>>(src, K, ld, cols, rowmax);
+    rowmax_kernel<<<dim3((unsigned)bx, (unsigned)by), 256, 0, s>>>(src, K, ld, cols, rowmax, rowmin);
+}
+
+void launch_decide_f64_path(const unsigned long long* rowmax, const unsigned long long* rowmin, long long K, int* gate,
+                            cudaStream_t s) {
+    decide_kernel<<<1, 256, 0, s>>>(rowmax, rowmin, K, gate);
 }
 
 void launch_load_rows_df(const double* src, long long K, long long ld, long long R, int mode, long long div,
                          const uint32_t* tab, void* dst, long long stride, int add,
-                         const unsigned long long* rowmax, cudaStream_t s) {
+                         const unsigned long long* rowmax, cudaStream_t s, const int* gate) {
     if (R <= 0) return;
     const dim3 grid((unsigned)((R + 31) / 32), (unsigned)((stride + 31) / 32));
     load_rows_df_kernel<<<grid, dim3(32, 8), 0, s>>>(src, K, ld, R, mode, div, tab, static_cast<DF*>(dst), stride,
-                                                     add, rowmax);
+                                                     add, rowmax, gate);
 }
 
 void launch_store_cols_df(const void* vals, long long stride, long long K, long long C, int mode, long long fold,
                           const uint32_t* tab, double* out, long long ld, int add,
-                          const unsigned long long* rowmax, cudaStream_t s) {
+                          const unsigned long long* rowmax, cudaStream_t s, const int* gate) {
     if (C <= 0 || K <= 0) return;
     const dim3 grid((unsigned)((C + 31) / 32), (unsigned)((K + 31) / 32));
     store_cols_df_kernel<<<grid, dim3(32, 8), 0, s>>>(static_cast<const DF*>(vals), stride, K, C, mode, fold, tab,
-                                                      out, ld, add, rowmax);
+                                                      out, ld, add, rowmax, gate);
 }
 
 void launch_init_vector_df(const double* init, long long K, long long n, void* vals, long long stride,
-                           const unsigned long long* rowmax, cudaStream_t s) {
-    init_vector_df_kernel<<<grid_for(n * stride), 256, 0, s>>>(init, K, n, static_cast<DF*>(vals), stride, rowmax);
+                           const unsigned long long* rowmax, cudaStream_t s, const int* gate) {
+    init_vector_df_kernel<<<grid_for(n * stride), 256, 0, s>>>(init, K, n, static_cast<DF*>(vals), stride, rowmax,
+                                                               gate);
 }
 
 void launch_init_xtx_df(const uint32_t* xtx, long long K, long long n, void* vals, long long stride,
-                        const unsigned long long* rowmax, cudaStream_t s) {
-    init_xtx_df_kernel<<<grid_for(n * stride), 256, 0, s>>>(xtx, K, n, static_cast<DF*>(vals), stride, rowmax);
+                        const unsigned long long* rowmax, cudaStream_t s, const int* gate) {
+    init_xtx_df_kernel<<<grid_for(n * stride), 256, 0, s>>>(xtx, K, n, static_cast<DF*>(vals), stride, rowmax, gate);
 }
 
 }  // namespace grgx

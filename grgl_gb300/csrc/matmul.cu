@@ -196,45 +196,52 @@ SweepParams<S> make_params(const DevCSR& c, long long cb, long long ce, const vo
     p.tickets = tickets;
     p.work = work;
     p.ntiles = ntiles;
+    p.gate = nullptr;
+    p.gate_value = 0;
     return p;
 }
 
 // Launches one level of a CSR; returns the number of kernels launched (0 or 1).
 // `work` points at L.ntiles zeroed counters owned by this launch.
 int launch_level(const Layout& L, const DevCSR& c, size_t level, const void* src, void* dst, int rmw,
-                 void* partials, unsigned* tickets, unsigned* work, cudaStream_t s) {
+                 void* partials, unsigned* tickets, unsigned* work, cudaStream_t s, const int* gate = nullptr,
+                 int gateValue = 0) {
     const long long cb = c.lb[level], ce = c.le[level];
     if (ce <= cb) return 0;
     const dim3 grid(static_cast<unsigned>((ce - cb + 7) / 8), static_cast<unsigned>(L.ntiles));
     const int sms = sm_count();
+    auto gated = [&](auto p) {
+        p.gate = gate;
+        p.gate_value = gateValue;
+        return p;
+    };
     switch (L.kind) {
     case Kind::U32:
-        launch_sweep_u32(make_params<uint32_t>(c, cb, ce, src, dst, L.stride, rmw, partials, tickets, work, L.ntiles),
+        launch_sweep_u32(gated(make_params<uint32_t>(c, cb, ce, src, dst, L.stride, rmw, partials, tickets, work, L.ntiles)),
                          L.vw, L.g, grid, sms, s);
         break;
     case Kind::XOR:
-        launch_sweep_xor(make_params<uint32_t>(c, cb, ce, src, dst, L.stride, rmw, partials, tickets, work, L.ntiles),
+        launch_sweep_xor(gated(make_params<uint32_t>(c, cb, ce, src, dst, L.stride, rmw, partials, tickets, work, L.ntiles)),
                          L.vw, L.g, grid, sms, s);
         break;
     case Kind::U64:
-        launch_sweep_u64(
-            make_params<unsigned long long>(c, cb, ce, src, dst, L.stride, rmw, partials, tickets, work, L.ntiles), L.vw,
+        launch_sweep_u64(gated(make_params<unsigned long long>(c, cb, ce, src, dst, L.stride, rmw, partials, tickets, work, L.ntiles)), L.vw,
             L.g, grid, sms, s);
         break;
     case Kind::F64:
-        launch_sweep_f64(make_params<double>(c, cb, ce, src, dst, L.stride, rmw, partials, tickets, work, L.ntiles),
+        launch_sweep_f64(gated(make_params<double>(c, cb, ce, src, dst, L.stride, rmw, partials, tickets, work, L.ntiles)),
                          L.vw, L.g, grid, sms, s);
         break;
     case Kind::F32C:
-        launch_sweep_f32c(make_params<float>(c, cb, ce, src, dst, L.stride, rmw, partials, tickets, work, L.ntiles),
+        launch_sweep_f32c(gated(make_params<float>(c, cb, ce, src, dst, L.stride, rmw, partials, tickets, work, L.ntiles)),
                           L.vw, L.g, grid, sms, s);
         break;
     case Kind::F32:
-        launch_sweep_f32(make_params<float>(c, cb, ce, src, dst, L.stride, rmw, partials, tickets, work, L.ntiles),
+        launch_sweep_f32(gated(make_params<float>(c, cb, ce, src, dst, L.stride, rmw, partials, tickets, work, L.ntiles)),
                          L.vw, L.g, grid, sms, s);
         break;
     case Kind::F64S:
-        launch_sweep_f64s(make_params<DF>(c, cb, ce, src, dst, L.stride, rmw, partials, tickets, work, L.ntiles),
+        launch_sweep_f64s(gated(make_params<DF>(c, cb, ce, src, dst, L.stride, rmw, partials, tickets, work, L.ntiles)),
                           L.vw, L.g, grid, sms, s);
         break;
     }
@@ -405,102 +412,134 @@ void matmul_impl(grgx_graph* g, int dtype, const void* input, uint64_t in_cols, 
         GRGX_CUDA(cudaMemsetAsync(tickets, 0, counterBytes, s));
         unsigned* work = tickets + nh * L.ntiles;  // one set of L.ntiles counters per launch
 
-        // ---- float64 row scales: exponent of each row's largest finite magnitude -------------
+        // ---- float64: row scales and the device-side choice between the float-pair path (gate
+        // 0) and the FP64-pipe path (gate 1, for rows spanning too many binades) ---------------
         unsigned long long* rowmax = nullptr;
+        int* gate = nullptr;
         if (df) {
-            rowmax = static_cast<unsigned long long*>(sc.get(static_cast<size_t>(K) * sizeof(unsigned long long)));
+            rowmax = static_cast<unsigned long long*>(sc.get(2 * static_cast<size_t>(K) * sizeof(unsigned long long)));
+            unsigned long long* rowmin = rowmax + K;
+            gate = static_cast<int*>(sc.get(sizeof(int)));
             unsigned long long floor = 0;
             if (init_kind == GRGX_INIT_XTX) std::memcpy(&floor, &dp->xtx_max, sizeof(floor));
             launch_fill_u64(rowmax, K, floor, s);
-            launch_rowmax(static_cast<const double*>(dIn), K, in_cols, in_cols, rowmax, s);
-            launches += 2;
-            if (init_kind == GRGX_INIT_VECTOR) launch_rowmax(static_cast<const double*>(dInit), K, 1, 1, rowmax, s);
-            if (init_kind == GRGX_INIT_MATRIX) launch_rowmax(static_cast<const double*>(dInit), K, n, n, rowmax, s);
-            if (down && dMiss) launch_rowmax(static_cast<const double*>(dMiss), K, M, M, rowmax, s);
-            launches += (init_kind == GRGX_INIT_VECTOR || init_kind == GRGX_INIT_MATRIX) + (down && dMiss);
-        }
-        auto load_rows = [&](const void* src, long long ld, long long R, int mode, long long div, const uint32_t* tab,
-                             void* dst, int add) {
-            if (df)
-                launch_load_rows_df(static_cast<const double*>(src), K, ld, R, mode, div, tab, dst, L.stride, add,
-                                    rowmax, s);
-            else
-                launch_load_rows(dtype, src, K, ld, R, mode, div, tab, dst, L.stride, add, s);
+            unsigned long long two = 0;  // smallest nonzero XTX value, 2 * one coalescence
+            const double twoD = 2.0;
+            std::memcpy(&two, &twoD, sizeof(two));
+            launch_fill_u64(rowmin, K, (init_kind == GRGX_INIT_XTX && floor) ? two : ~0ull, s);
+            launch_rowmax(static_cast<const double*>(dIn), K, in_cols, in_cols, rowmax, rowmin, s);
+            launches += 3;
+            if (init_kind == GRGX_INIT_VECTOR) {
+                launch_rowmax(static_cast<const double*>(dInit), K, 1, 1, rowmax, rowmin, s);
+                launches++;
+            }
+            if (init_kind == GRGX_INIT_MATRIX) {
+                launch_rowmax(static_cast<const double*>(dInit), K, n, n, rowmax, rowmin, s);
+                launches++;
+            }
+            if (down && dMiss) {
+                launch_rowmax(static_cast<const double*>(dMiss), K, M, M, rowmax, rowmin, s);
+                launches++;
+            }
+            launch_decide_f64_path(rowmax, rowmin, K, gate, s);
             launches++;
-        };
-        auto store_cols = [&](long long C, int mode, long long fold, const uint32_t* tab, void* out, long long ld,
-                              int add) {
-            if (df)
-                launch_store_cols_df(vals, L.stride, K, C, mode, fold, tab, static_cast<double*>(out), ld, add, rowmax,
-                                     s);
-            else
-                launch_store_cols(dtype, vals, L.stride, K, C, mode, fold, tab, out, ld, add, s);
-            launches++;
-        };
-
-        // ---- init -------------------------------------------------------------------------
-        switch (init_kind) {
-        case GRGX_INIT_VECTOR:
-            if (df)
-                launch_init_vector_df(static_cast<const double*>(dInit), K, n, vals, L.stride, rowmax, s);
-            else
-                launch_init_vector(dtype, dInit, K, n, vals, L.stride, s);
-            launches++;
-            break;
-        case GRGX_INIT_MATRIX: load_rows(dInit, n, n, MAP_TABLE, 1, dp->new2old, vals, 0); break;
-        case GRGX_INIT_XTX:
-            if (df)
-                launch_init_xtx_df(dp->xtx_new, K, n, vals, L.stride, rowmax, s);
-            else
-                launch_init_xtx(dtype, dp->xtx_new, K, n, vals, L.stride, s);
-            launches++;
-            break;
-        default: GRGX_CUDA(cudaMemsetAsync(vals, 0, valBytes, s)); break;
         }
         const int hasInit = (init_kind != GRGX_INIT_ZERO);
+        const int add = overwrite ? 0 : 1;
+        if (init_kind == GRGX_INIT_ZERO) GRGX_CUDA(cudaMemsetAsync(vals, 0, valBytes, s));
+        // Scratch shared by both float64 paths (same 8-byte elements).
+        void* vt = (down && dp->seed.n_edges > 0) ? sc.get(static_cast<size_t>(M) * L.stride * L.ssize) : nullptr;
+        void* mt = (down && useMiss && dp->miss.n_edges > 0) ? sc.get(static_cast<size_t>(M) * L.stride * L.ssize)
+                                                              : nullptr;
 
-        if (down) {
-            // ---- DOWN seed: mutation rows, then node <- sum of its mutations ---------------------
-            unsigned* tk = tickets;
-            if (dp->seed.n_edges > 0) {
-                void* vt = sc.get(static_cast<size_t>(M) * L.stride * L.ssize);
-                load_rows(dIn, in_cols, M, MAP_IDENT, 1, nullptr, vt, 0);
-                launches += launch_level(L, dp->seed, 0, vt, vals, hasInit, partials, tk, work, s);
+        // One full pipeline (init, seed, level sweep, gather) for layout LL; `pdf` selects the
+        // float-pair I/O kernels; kernels run only where *g == gv when g is set.
+        auto pipeline = [&](const Layout& LL, bool pdf, const int* g, int gv, bool timed) {
+            auto load_rows = [&](const void* src, long long ld, long long R, int mode, long long div,
+                                 const uint32_t* tab, void* dst, int addTo) {
+                if (pdf)
+                    launch_load_rows_df(static_cast<const double*>(src), K, ld, R, mode, div, tab, dst, LL.stride,
+                                        addTo, rowmax, s, g);
+                else
+                    launch_load_rows(dtype, src, K, ld, R, mode, div, tab, dst, LL.stride, addTo, s, g, gv);
+                launches++;
+            };
+            auto store_cols = [&](long long C, int mode, long long fold, const uint32_t* tab, void* out, long long ld,
+                                  int addTo) {
+                if (pdf)
+                    launch_store_cols_df(vals, LL.stride, K, C, mode, fold, tab, static_cast<double*>(out), ld, addTo,
+                                         rowmax, s, g);
+                else
+                    launch_store_cols(dtype, vals, LL.stride, K, C, mode, fold, tab, out, ld, addTo, s, g, gv);
+                launches++;
+            };
+            auto level = [&](const DevCSR& c, size_t lvl, const void* src, int rmw, unsigned* tk, unsigned* wk) {
+                return launch_level(LL, c, lvl, src, vals, rmw, partials, tk, wk, s, g, gv);
+            };
+            switch (init_kind) {
+            case GRGX_INIT_VECTOR:
+                if (pdf)
+                    launch_init_vector_df(static_cast<const double*>(dInit), K, n, vals, LL.stride, rowmax, s, g);
+                else
+                    launch_init_vector(dtype, dInit, K, n, vals, LL.stride, s, g, gv);
+                launches++;
+                break;
+            case GRGX_INIT_MATRIX: load_rows(dInit, n, n, MAP_TABLE, 1, dp->new2old, vals, 0); break;
+            case GRGX_INIT_XTX:
+                if (pdf)
+                    launch_init_xtx_df(dp->xtx_new, K, n, vals, LL.stride, rowmax, s, g);
+                else
+                    launch_init_xtx(dtype, dp->xtx_new, K, n, vals, LL.stride, s, g, gv);
+                launches++;
+                break;
+            default: break;
             }
-            tk += dp->seed.n_heavy * L.ntiles;
-            if (useMiss && dp->miss.n_edges > 0) {
-                void* mt = sc.get(static_cast<size_t>(M) * L.stride * L.ssize);
-                load_rows(dMiss, M, M, MAP_IDENT, 1, nullptr, mt, 0);
-                launches += launch_level(L, dp->miss, 0, mt, vals, 1, partials, tk, work + L.ntiles, s);
-            }
-            tk += dp->miss.n_heavy * L.ntiles;
-            if (t_timing) GRGX_CUDA(cudaEventRecord(ev[1], s));
-            for (size_t lvl = 0; lvl < dp->down.lb.size(); lvl++)
-                launches += launch_level(L, dp->down, lvl, vals, vals, 1, partials, tk, work + (2 + lvl) * L.ntiles, s);
-            if (t_timing) GRGX_CUDA(cudaEventRecord(ev[2], s));
-            // ---- gather samples -----------------------------------------------------------------
-            const int add = overwrite ? 0 : 1;
-            if (emit_all) {
-                store_cols(n, MAP_TABLE, 1, dp->old2new, dOut, out_cols, add);
-            } else if (by_indiv) {
-                store_cols(out_cols, MAP_FOLD, P, nullptr, dOut, out_cols, add);
+            if (down) {
+                // DOWN seed: mutation rows, then node <- sum of its mutations (and missingness)
+                unsigned* tk = tickets;
+                if (vt) {
+                    load_rows(dIn, in_cols, M, MAP_IDENT, 1, nullptr, vt, 0);
+                    launches += level(dp->seed, 0, vt, hasInit, tk, work);
+                }
+                tk += dp->seed.n_heavy * LL.ntiles;
+                if (mt) {
+                    load_rows(dMiss, M, M, MAP_IDENT, 1, nullptr, mt, 0);
+                    launches += level(dp->miss, 0, mt, 1, tk, work + LL.ntiles);
+                }
+                tk += dp->miss.n_heavy * LL.ntiles;
+                if (timed && t_timing) GRGX_CUDA(cudaEventRecord(ev[1], s));
+                for (size_t lvl = 0; lvl < dp->down.lb.size(); lvl++)
+                    launches += level(dp->down, lvl, vals, 1, tk, work + (2 + lvl) * LL.ntiles);
+                if (timed && t_timing) GRGX_CUDA(cudaEventRecord(ev[2], s));
+                if (emit_all) {
+                    store_cols(n, MAP_TABLE, 1, dp->old2new, dOut, out_cols, add);
+                } else if (by_indiv) {
+                    store_cols(out_cols, MAP_FOLD, P, nullptr, dOut, out_cols, add);
+                } else {
+                    store_cols(out_cols, MAP_IDENT, 1, nullptr, dOut, out_cols, add);
+                }
             } else {
-                store_cols(out_cols, MAP_IDENT, 1, nullptr, dOut, out_cols, add);
+                // UP seed: samples <- input columns
+                load_rows(dIn, in_cols, N, by_indiv ? MAP_DIV : MAP_IDENT, P, nullptr, vals, hasInit);
+                if (timed && t_timing) GRGX_CUDA(cudaEventRecord(ev[1], s));
+                for (size_t lvl = 0; lvl < dp->up.lb.size(); lvl++)
+                    launches += level(dp->up, lvl, vals, hasInit, tickets, work + lvl * LL.ntiles);
+                if (timed && t_timing) GRGX_CUDA(cudaEventRecord(ev[2], s));
+                if (emit_all) {
+                    store_cols(n, MAP_TABLE, 1, dp->old2new, dOut, out_cols, add);
+                } else {
+                    store_cols(M, MAP_TABLE, 1, dp->mut_new, dOut, out_cols, add);
+                    if (useMiss) store_cols(M, MAP_TABLE, 1, dp->miss_new, dMiss, M, 1);
+                }
             }
+        };
+        if (df) {
+            Layout LN = L;
+            LN.kind = Kind::F64;
+            pipeline(L, true, gate, 0, true);
+            pipeline(LN, false, gate, 1, false);
         } else {
-            // ---- UP seed: samples <- input columns -------------------------------------------------
-            load_rows(dIn, in_cols, N, by_indiv ? MAP_DIV : MAP_IDENT, P, nullptr, vals, hasInit);
-            if (t_timing) GRGX_CUDA(cudaEventRecord(ev[1], s));
-            for (size_t lvl = 0; lvl < dp->up.lb.size(); lvl++)
-                launches += launch_level(L, dp->up, lvl, vals, vals, hasInit, partials, tickets, work + lvl * L.ntiles, s);
-            if (t_timing) GRGX_CUDA(cudaEventRecord(ev[2], s));
-            const int add = overwrite ? 0 : 1;
-            if (emit_all) {
-                store_cols(n, MAP_TABLE, 1, dp->old2new, dOut, out_cols, add);
-            } else {
-                store_cols(M, MAP_TABLE, 1, dp->mut_new, dOut, out_cols, add);
-                if (useMiss) store_cols(M, MAP_TABLE, 1, dp->miss_new, dMiss, M, 1);
-            }
+            pipeline(L, false, nullptr, 0, true);
         }
         GRGX_CUDA(cudaGetLastError());
         if (!devPtrs) {

@@ -45,6 +45,8 @@ template <typename S> struct SweepParams {
     unsigned* tickets;         // per (heavy row, column tile)
     unsigned* work;            // per column tile: next chunk to take (zeroed before the launch)
     int ntiles;
+    const int* gate;           // when set, the launch runs only if *gate == gate_value
+    int gate_value;
 };
 
 template <typename S, int VW> struct Vec;
@@ -310,6 +312,7 @@ template <class Op, int VW, int G> struct SweepOccupancy {
 
 template <class Op, int VW, int G>
 __global__ void __launch_bounds__(256, SweepOccupancy<Op, VW, G>::kBlocks) sweep_kernel(const SweepParams<typename Op::S> p) {
+    if (p.gate != nullptr && *p.gate != p.gate_value) return;
     const int lane = threadIdx.x & 31;
     unsigned* counter = p.work + blockIdx.y;
     for (;;) {
