@@ -214,4 +214,69 @@ struct AddF64S {
     }
 };
 
+// ---- packed float2 arithmetic (Blackwell FADD2 / FFMA2) ---------------------------------------
+// Two float additions per instruction; a - b is formed as fma(b, -1, a), which is exact before
+// the single rounding, so every operation rounds exactly like the scalar __fadd_rn/__fsub_rn.
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.0f, -1.0f), a); }
+
+// acc[i] += v[i] for a lane's VW columns; the compensated operators use packed pairs.
+template <class Op, int VW> struct VecAdd {
+    static __device__ __forceinline__ void add(typename Op::A* acc, const typename Op::S* v) {
+#pragma unroll
+        for (int i = 0; i < VW; i++) Op::add(acc[i], v[i]);
+    }
+};
+
+template <int VW> struct VecAdd<AddF32C, VW> {
+    static __device__ __forceinline__ void add(F32Pair* acc, const float* v) {
+        if constexpr (VW % 2 == 0) {
+#pragma unroll
+            for (int j = 0; j < VW; j += 2) {
+                const float2 a = make_float2(acc[j].hi, acc[j + 1].hi);
+                const float2 b = make_float2(v[j], v[j + 1]);
+                const float2 s = add2(a, b);
+                const float2 bb = sub2(s, a);
+                const float2 e = add2(sub2(a, sub2(s, bb)), sub2(b, bb));
+                const float2 lo = add2(make_float2(acc[j].lo, acc[j + 1].lo), e);
+                acc[j] = {s.x, lo.x};
+                acc[j + 1] = {s.y, lo.y};
+            }
+        } else {
+#pragma unroll
+            for (int i = 0; i < VW; i++) AddF32C::add(acc[i], v[i]);
+        }
+    }
+};
+
+template <int VW> struct VecAdd<AddF64S, VW> {
+    static __device__ __forceinline__ void add(F64Run* acc, const DF* v) {
+        if constexpr (VW % 2 == 0) {
+#pragma unroll
+            for (int j = 0; j < VW; j += 2) {
+                const float2 hi = make_float2(acc[j].hi, acc[j + 1].hi);
+                const float2 lo = make_float2(acc[j].lo, acc[j + 1].lo);
+                const float2 xh = make_float2(v[j].hi, v[j + 1].hi);
+                const float2 xl = make_float2(v[j].lo, v[j + 1].lo);
+                const float2 s = add2(hi, xh);
+                const float2 bb = sub2(s, hi);
+                float2 e = add2(sub2(hi, sub2(s, bb)), sub2(xh, bb));
+                e = add2(e, add2(lo, xl));
+                const float2 nh = add2(s, e);
+                const float2 nl = sub2(e, sub2(nh, s));
+                const float2 p = add2(make_float2(acc[j].p, acc[j + 1].p), xh);
+                acc[j].hi = nh.x;
+                acc[j + 1].hi = nh.y;
+                acc[j].lo = nl.x;
+                acc[j + 1].lo = nl.y;
+                acc[j].p = p.x;
+                acc[j + 1].p = p.y;
+            }
+        } else {
+#pragma unroll
+            for (int i = 0; i < VW; i++) AddF64S::add(acc[i], v[i]);
+        }
+    }
+};
+
 }  // namespace grgx

@@ -203,10 +203,7 @@ __device__ __forceinline__ void sweep_chunk(const SweepParams<typename Op::S>& p
             if (anyHead == 0u) {
                 // no row starts in this step: every edge continues the current row
 #pragma unroll
-                for (int u = 0; u < BATCH; u++) {
-#pragma unroll
-                    for (int i = 0; i < VW; i++) Op::add(acc[i], v[u][i]);
-                }
+                for (int u = 0; u < BATCH; u++) VecAdd<Op, VW>::add(acc, v[u]);
                 continue;
             }
 #pragma unroll
@@ -215,8 +212,7 @@ __device__ __forceinline__ void sweep_chunk(const SweepParams<typename Op::S>& p
                 const int b = t / G, s = t % G;
                 const unsigned hs = (NG == 32) ? heads[b] : ((heads[b] >> (s * NG)) & NGMASK);
                 if (hs == 0u) {
-#pragma unroll
-                    for (int i = 0; i < VW; i++) Op::add(acc[i], v[u][i]);
+                    VecAdd<Op, VW>::add(acc, v[u]);
                     continue;
                 }
                 const int q = __popc(hs & upto);  // rows started at or before my edge
