@@ -1,0 +1,70 @@
+// Device-resident plan and launch helpers shared by the matmul entry points (internal).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "grgx_internal.h"
+#include "launch.h"
+
+namespace grgx {
+
+#define GRGX_CUDA(call)                                                                               \
+    do {                                                                                             \
+        cudaError_t err__ = (call);                                                                  \
+        if (err__ != cudaSuccess) {                                                                  \
+            const int code__ = (err__ == cudaErrorMemoryAllocation) ? GRGX_ERR_OUT_OF_MEMORY         \
+                                                                    : GRGX_ERR_CUDA;                 \
+            throw ::grgx::Error(code__, std::string(#call) + ": " + cudaGetErrorString(err__));       \
+        }                                                                                            \
+    } while (0)
+
+struct DevCSR {
+    uint32_t* adj = nullptr;
+    int* rows = nullptr;
+    ChunkDev* chunks = nullptr;
+    HeavyDev* heavy = nullptr;
+    std::vector<int32_t> lb, le;
+    long long n_heavy = 0, n_pieces = 0, n_edges = 0, n_rows = 0;
+};
+
+struct DevicePlan {
+    int device = -1;
+    DevCSR up, down, seed, miss;
+    uint32_t* mut_new = nullptr;
+    uint32_t* miss_new = nullptr;
+    uint32_t* old2new = nullptr;
+    uint32_t* new2old = nullptr;
+    uint32_t* xtx_new = nullptr;
+    uint64_t bytes = 0;
+    uint64_t num_levels = 0;
+    bool has_coals = false;
+    bool has_miss = false;
+    double xtx_max = 0.0;  // largest XTX init value (2 * coalescences)
+    std::vector<void*> allocs;
+};
+
+struct Layout {
+    Kind kind;
+    int ssize;     // storage bytes per element
+    int asize;     // accumulator bytes per element (heavy partials)
+    long long stride;
+    int vw, g, ntiles;
+};
+
+// Element layout of one call: storage kind, row stride and the (VW, G) sweep shape.
+Layout choose_layout(int dtype, long long K, bool plainF32, bool nativeF64);
+
+int sm_count();
+
+// Launches one level of a CSR (a no-op when the level has no chunks); `work` points at
+// L.ntiles zeroed counters owned by this launch.  Returns the number of kernels launched.
+int launch_level(const Layout& L, const DevCSR& c, size_t level, const void* src, void* dst, int rmw,
+                 void* partials, unsigned* tickets, unsigned* work, cudaStream_t s, const int* gate = nullptr,
+                 int gateValue = 0);
+
+// Builds (once) and returns the graph's plan on the current device.
+DevicePlan* ensure_device_plan(grgx_graph* g);
+
+}  // namespace grgx

@@ -16,44 +16,11 @@
 #include <thread>
 
 #include "grgx_internal.h"
+#include "device_plan.h"
 #include "launch.h"
 
 namespace grgx {
 
-#define GRGX_CUDA(call)                                                                               \
-    do {                                                                                             \
-        cudaError_t err__ = (call);                                                                  \
-        if (err__ != cudaSuccess) {                                                                  \
-            const int code__ = (err__ == cudaErrorMemoryAllocation) ? GRGX_ERR_OUT_OF_MEMORY         \
-                                                                    : GRGX_ERR_CUDA;                 \
-            throw ::grgx::Error(code__, std::string(#call) + ": " + cudaGetErrorString(err__));       \
-        }                                                                                            \
-    } while (0)
-
-struct DevCSR {
-    uint32_t* adj = nullptr;
-    int* rows = nullptr;
-    ChunkDev* chunks = nullptr;
-    HeavyDev* heavy = nullptr;
-    std::vector<int32_t> lb, le;
-    long long n_heavy = 0, n_pieces = 0, n_edges = 0, n_rows = 0;
-};
-
-struct DevicePlan {
-    int device = -1;
-    DevCSR up, down, seed, miss;
-    uint32_t* mut_new = nullptr;
-    uint32_t* miss_new = nullptr;
-    uint32_t* old2new = nullptr;
-    uint32_t* new2old = nullptr;
-    uint32_t* xtx_new = nullptr;
-    uint64_t bytes = 0;
-    uint64_t num_levels = 0;
-    bool has_coals = false;
-    bool has_miss = false;
-    double xtx_max = 0.0;  // largest XTX init value (2 * coalescences)
-    std::vector<void*> allocs;
-};
 
 void destroy_device_plan(DevicePlan* p) {
     if (!p) return;
@@ -108,13 +75,7 @@ void setup_pool_once(int device) {
     done.push_back(device);
 }
 
-struct Layout {
-    Kind kind;
-    int ssize;     // storage bytes per element
-    int asize;     // accumulator bytes per element (heavy partials)
-    long long stride;
-    int vw, g, ntiles;
-};
+}  // namespace
 
 long long next_pow2(long long x) {
     long long p = 1;
@@ -148,6 +109,8 @@ Layout choose_layout(int dtype, long long K, bool plainF32, bool nativeF64) {
     return L;
 }
 
+namespace {
+
 struct Scratch {
     cudaStream_t s;
     std::vector<void*> ptrs;
@@ -166,6 +129,8 @@ struct Scratch {
 
 thread_local bool t_timing = false;
 thread_local grgx_timing t_last{};
+
+}  // namespace
 
 int sm_count() {
     static int sms = 0;
@@ -204,8 +169,8 @@ SweepParams<S> make_params(const DevCSR& c, long long cb, long long ce, const vo
 // Launches one level of a CSR; returns the number of kernels launched (0 or 1).
 // `work` points at L.ntiles zeroed counters owned by this launch.
 int launch_level(const Layout& L, const DevCSR& c, size_t level, const void* src, void* dst, int rmw,
-                 void* partials, unsigned* tickets, unsigned* work, cudaStream_t s, const int* gate = nullptr,
-                 int gateValue = 0) {
+                 void* partials, unsigned* tickets, unsigned* work, cudaStream_t s, const int* gate,
+                 int gateValue) {
     const long long cb = c.lb[level], ce = c.le[level];
     if (ce <= cb) return 0;
     const dim3 grid(static_cast<unsigned>((ce - cb + 7) / 8), static_cast<unsigned>(L.ntiles));
@@ -247,6 +212,8 @@ int launch_level(const Layout& L, const DevCSR& c, size_t level, const void* src
     }
     return 1;
 }
+
+namespace {
 
 size_t io_size(int dtype) {
     switch (dtype) {
