@@ -44,6 +44,11 @@ def parse_args():
     ap.add_argument("--dtypes", default="int32,float32,float64")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline sample budget")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end pass")
+    ap.add_argument("--only", default=None,
+                    help="restrict the step to dtype:K:dir entries, e.g. float32:64:UP,int32:1:DOWN")
+    ap.add_argument("--breakdown", action="store_true",
+                    help="print per-matmul device times (3 calls each, CUDA events) instead of the JSON line")
     return ap.parse_args()
 
 
@@ -55,6 +60,12 @@ def dist_env():
 
 
 def workload(args):
+    if args.only:
+        out = []
+        for item in args.only.split(","):
+            dt, K, d = item.split(":")
+            out.append((np.dtype(dt), int(K), UP if d.upper() == "UP" else DOWN))
+        return out
     ks = [int(k) for k in args.ks.split(",")]
     dts = [np.dtype(d) for d in args.dtypes.split(",")]
     return [(dt, K, d) for dt in dts for K in ks for d in (UP, DOWN)]
@@ -215,6 +226,21 @@ def main():
                 t = gx.last_timing()
                 record.append((dt, K, d, t))
 
+    if args.breakdown:
+        gx.set_timing(True)
+        E = stats["edges"]
+        print(json.dumps({"graph": stats}), flush=True)
+        for (dt, K, d), V in zip(combos, dev_inputs):
+            for _ in range(3):
+                gx.matmul(g, V, d)
+            t = gx.last_timing()
+            rec = {"dtype": str(dt), "K": K, "dir": "UP" if d == UP else "DOWN", "total_ms": t["total_ms"],
+                   "sweep_ms": t["sweep_ms"], "edgeK_per_s": E * K / (t["sweep_ms"] / 1e3),
+                   "gathered_GBps": E * (4 + K * dt.itemsize) / (t["sweep_ms"] / 1e3) / 1e9,
+                   "launches": t["launches"]}
+            print(json.dumps(rec), flush=True)
+        return
+
     # warm-up
     for _ in range(args.warmup):
         step(dev_inputs, None)
@@ -260,13 +286,15 @@ def main():
     barrier()
     h2d = sum(V.nbytes for V in host_inputs)
     d2h = sum(K * (stats["mutations"] if d == UP else stats["samples"]) * dt.itemsize for dt, K, d in combos)
-    t0 = time.perf_counter()
-    e2e_steps = max(1, min(args.steps, 2))
-    for _ in range(e2e_steps):
-        step(host_inputs, None)
-    barrier()
-    e2e_s = time.perf_counter() - t0
-    e2e_value = units_per_step * e2e_steps * world / e2e_s
+    e2e_value = None
+    if not args.no_e2e:
+        t0 = time.perf_counter()
+        e2e_steps = max(1, min(args.steps, 2))
+        for _ in range(e2e_steps):
+            step(host_inputs, None)
+        barrier()
+        e2e_s = time.perf_counter() - t0
+        e2e_value = units_per_step * e2e_steps * world / e2e_s
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
