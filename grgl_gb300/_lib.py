@@ -13,6 +13,7 @@ LIB_PATH = Path(__file__).resolve().parent / "libgrgx.so"
 
 OK, ERR_API_MISUSE, ERR_CUDA, ERR_OOM, ERR_BAD_FILE, ERR_UNSUPPORTED, ERR_NO_DEVICE, ERR_TIMEOUT = range(8)
 FLAG_DEVICE_POINTERS, FLAG_F32_PLAIN, FLAG_SYNC, FLAG_OVERWRITE, FLAG_F64_NATIVE = 0x1, 0x2, 0x4, 0x8, 0x10
+NOALLOC_SCRATCH_BYTES = 64 << 20  # GRGX_NOALLOC_SCRATCH_BYTES
 
 # Every symbol include/grgx.h declares, with its ctypes signature.
 c_graph_p = ctypes.c_void_p
@@ -41,6 +42,7 @@ SIGNATURES = {
     "grgx_graph_upload": (_int, [c_graph_p]),
     "grgx_matmul": (_int, [c_graph_p, _int, _vp, _u64, _u64, _int, _vp, _u64, _int, _int, _vp, _int, _vp, _u32,
                            _vp]),
+    "grgx_matmul_noalloc": (_int, [c_graph_p, _int, _vp, _u64, _u64, _int, _vp, _u64, _vp]),
     "grgx_set_timing": (None, [_int]),
     "grgx_last_timing": (_int, [ctypes.POINTER(Timing)]),
 }

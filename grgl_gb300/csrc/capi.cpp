@@ -14,6 +14,8 @@ void matmul_impl(grgx_graph* g, int dtype, const void* input, uint64_t in_cols, 
                  void* miss, uint32_t flags, void* stream);
 void set_timing(int enabled);
 grgx_timing last_timing();
+void matmul_noalloc_impl(grgx_graph* g, int dtype, const void* input, uint64_t in_cols, uint64_t rows, int direction,
+                         void* output, uint64_t output_size, void* stream);
 
 namespace {
 thread_local std::string t_error;
@@ -192,6 +194,15 @@ grgx_status grgx_matmul(grgx_graph* g, grgx_dtype dtype, const void* input, uint
         GRGX_CHECK(g && input && output, GRGX_ERR_API_MISUSE, "null argument");
         matmul_impl(g, dtype, input, input_cols, input_rows, direction, output, output_size, emit_all_nodes,
                     by_individual, init, init_kind, miss, flags, stream);
+    });
+}
+
+grgx_status grgx_matmul_noalloc(grgx_graph* g, grgx_dtype dtype, const void* input, uint64_t input_cols,
+                                uint64_t input_rows, grgx_direction direction, void* output, uint64_t output_size,
+                                void* stream) {
+    return guarded([&] {
+        GRGX_CHECK(g && input && output, GRGX_ERR_API_MISUSE, "null argument");
+        matmul_noalloc_impl(g, dtype, input, input_cols, input_rows, direction, output, output_size, stream);
     });
 }
 

@@ -133,6 +133,24 @@ grgx_status grgx_matmul(grgx_graph* g, grgx_dtype dtype, const void* input, uint
                         int emit_all_nodes, int by_individual, const void* init, grgx_init init_kind, void* miss,
                         uint32_t flags, void* stream);
 
+/* Size of the static device scratch behind grgx_matmul_noalloc (64 MiB on every GPU that loads
+ * the library, held until the process exits). */
+#define GRGX_NOALLOC_SCRATCH_BYTES (64ull << 20)
+
+/* No counterpart in the reference.  The plain product (no init, miss, emit_all_nodes or
+ * by_individual) for callers that cannot allocate device memory once they are running -- for
+ * example a host program that hands out a fixed device budget at start-up and forbids
+ * allocation afterwards.  It allocates nothing: its scratch is one static __device__ array of
+ * GRGX_NOALLOC_SCRATCH_BYTES, and products that need more are rejected with
+ * GRGX_ERR_UNSUPPORTED before any launch.  input/output are device pointers; the output is
+ * overwritten; the call is asynchronous on `stream`.  The graph must already be resident
+ * (grgx_graph_upload).  The first call on each device looks up the array's address; make it
+ * before any stream capture.  All calls share the array: calls that overlap on the GPU race,
+ * so serialise them on one stream.  bool is not supported. */
+grgx_status grgx_matmul_noalloc(grgx_graph* g, grgx_dtype dtype, const void* input, uint64_t input_cols,
+                                uint64_t input_rows, grgx_direction direction, void* output, uint64_t output_size,
+                                void* stream);
+
 /* Device-time breakdown of the last grgx_matmul made by this thread with timing enabled. */
 typedef struct {
     float total_ms;     /* seed + sweep + gather, CUDA events */
