@@ -306,7 +306,8 @@ def main():
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "int32,float32,float64", "data": "synthetic (seeded window-tree GRG)",
             "config": {"workload": f"plain matmul, window-tree GRG N={args.samples} M={args.mutations} seed={args.seed}, "
-                                   f"K in {{{args.ks}}}, UP+DOWN, {args.dtypes}; 24 matmuls per step",
+                                   + (f"K in {{{args.ks}}}, UP+DOWN, {args.dtypes}" if not args.only else args.only)
+                                   + f"; {len(combos)} matmuls per step",
                        "graph": stats, "l2": "inputs larger than L2 (edge CSR streamed every traversal)",
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
