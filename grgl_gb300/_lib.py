@@ -30,6 +30,16 @@ class Timing(ctypes.Structure):
                 ("alg_bytes", _u64)]
 
 
+class Request(ctypes.Structure):
+    _fields_ = [("dtype", ctypes.c_int), ("direction", ctypes.c_int), ("rows", _u64), ("input", _vp),
+                ("output", _vp)]
+
+
+class RequestStats(ctypes.Structure):
+    _fields_ = [("submit_s", ctypes.c_double), ("start_s", ctypes.c_double), ("done_s", ctypes.c_double),
+                ("batch_requests", _u64), ("batch_rows", _u64)]
+
+
 SIGNATURES = {
     "grgx_last_error": (ctypes.c_char_p, []),
     "grgx_version": (ctypes.c_char_p, []),
@@ -43,6 +53,12 @@ SIGNATURES = {
     "grgx_matmul": (_int, [c_graph_p, _int, _vp, _u64, _u64, _int, _vp, _u64, _int, _int, _vp, _int, _vp, _u32,
                            _vp]),
     "grgx_matmul_noalloc": (_int, [c_graph_p, _int, _vp, _u64, _u64, _int, _vp, _u64, _vp]),
+    "grgx_matmul_batch": (_int, [c_graph_p, ctypes.POINTER(Request), _u64, _u64, _u32, _vp]),
+    "grgx_server_create": (_int, [_u32, _u64, _u64, ctypes.POINTER(_vp)]),
+    "grgx_server_add_graph": (_int, [_vp, c_graph_p, ctypes.POINTER(_u32)]),
+    "grgx_server_submit": (_int, [_vp, _u32, ctypes.POINTER(Request), ctypes.POINTER(_u64)]),
+    "grgx_server_wait": (_int, [_vp, _u64, ctypes.c_double, ctypes.POINTER(RequestStats)]),
+    "grgx_server_destroy": (None, [_vp]),
     "grgx_set_timing": (None, [_int]),
     "grgx_last_timing": (_int, [ctypes.POINTER(Timing)]),
 }

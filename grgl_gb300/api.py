@@ -343,3 +343,115 @@ def last_timing() -> dict:
     _lib.check(_lib.lib().grgx_last_timing(ctypes.byref(t)))
     return {"total_ms": t.total_ms, "sweep_ms": t.sweep_ms, "launches": int(t.launches),
             "alg_bytes": int(t.alg_bytes)}
+
+
+# ---- batching and serving ----------------------------------------------------------------------
+
+
+def _request_for(grg, x, direction):
+    """Validate one plain request and allocate its output (host or device like the input)."""
+    direction = TraversalDirection(int(direction))
+    cols = grg.num_samples if direction == UP else grg.num_mutations
+    out_cols = grg.num_mutations if direction == UP else grg.num_samples
+    if _is_torch_cuda(x):
+        import torch
+
+        x = x.contiguous()
+        npd = _torch_dtype_to_np(x.dtype)
+        _check(npd is not None, f"Unsupported dtype: {x.dtype}")
+        _check(x.dim() == 2 and x.shape[0] > 0 and x.shape[1] == cols,
+               "Input vector is not size N (numSamples, or numIndividuals depending on flags)" if direction == UP
+               else "Input vector is not size M (numMutations)")
+        out = torch.empty((x.shape[0], out_cols), dtype=x.dtype, device=x.device)
+        code = _DTYPE_CODES[np.dtype(npd)]
+        return x, out, _lib.Request(code, int(direction), x.shape[0], x.data_ptr(), out.data_ptr())
+    _check(isinstance(x, np.ndarray), f"Unsupported numpy dtype: {np.asarray(x).dtype}")
+    x = np.ascontiguousarray(x)
+    _check(x.ndim == 2, "matmul() only support two dimensional numpy arrays as input.")
+    _check(x.dtype in _DTYPE_CODES, f"Unsupported numpy dtype: {x.dtype}")
+    _check(x.shape[0] > 0 and x.shape[1] > 0, "matmul() requires non-zero dimensions.")
+    _check(x.shape[1] == cols,
+           "Input vector is not size N (numSamples, or numIndividuals depending on flags)" if direction == UP
+           else "Input vector is not size M (numMutations)")
+    out = np.empty((x.shape[0], out_cols), dtype=x.dtype)
+    return x, out, _lib.Request(_DTYPE_CODES[x.dtype], int(direction), x.shape[0], x.ctypes.data, out.ctypes.data)
+
+
+def matmul_batch(grg: GRG, requests, max_cols: int = 0, *, f32_compensated: bool = True, f64_native: bool = False):
+    """Several plain products on one graph, coalesced into shared traversals.
+
+    ``requests`` is a list of ``(input, direction)``; inputs are all numpy arrays or all CUDA
+    tensors.  Returns the outputs in order.  Requests of the same direction and dtype are
+    stacked into traversals of at most ``max_cols`` rows (0 = the sweep's natural width).
+    """
+    prepared = [_request_for(grg, x, d) for x, d in requests]
+    if not prepared:
+        return []
+    dev = _is_torch_cuda(prepared[0][0])
+    _check(all(_is_torch_cuda(p[0]) == dev for p in prepared), "inputs must be all host or all device arrays")
+    arr = (_lib.Request * len(prepared))(*[p[2] for p in prepared])
+    flags = _flags(f32_compensated, f64_native)
+    stream = None
+    if dev:
+        import torch
+
+        flags |= _lib.FLAG_DEVICE_POINTERS
+        stream = torch.cuda.current_stream(prepared[0][0].device).cuda_stream
+    _lib.check(_lib.lib().grgx_matmul_batch(grg._h, arr, len(prepared), max_cols, flags, stream))
+    return [p[1] for p in prepared]
+
+
+class Server:
+    """Serving loop with continuous batching over resident graphs (native worker threads).
+
+    ``submit`` queues a plain product and returns a ticket; ``result`` waits for it and returns
+    ``(output, stats)`` where stats has the submit/start/done times (seconds since the server
+    started) and the size of the batch the request ran in.
+    """
+
+    def __init__(self, workers: int = 2, memory_budget: int = 0, max_cols: int = 0):
+        h = ctypes.c_void_p()
+        _lib.check(_lib.lib().grgx_server_create(workers, memory_budget, max_cols, ctypes.byref(h)))
+        self._h = h
+        self._graphs = []
+        self._live = {}
+
+    def add_graph(self, grg: GRG) -> int:
+        gid = ctypes.c_uint32()
+        _lib.check(_lib.lib().grgx_server_add_graph(self._h, grg._h, ctypes.byref(gid)))
+        self._graphs.append(grg)
+        return int(gid.value)
+
+    def submit(self, graph_id: int, input, direction) -> int:
+        x, out, req = _request_for(self._graphs[graph_id], input, direction)
+        _check(not _is_torch_cuda(x), "the server takes host (numpy) arrays")
+        t = ctypes.c_uint64()
+        _lib.check(_lib.lib().grgx_server_submit(self._h, graph_id, ctypes.byref(req), ctypes.byref(t)))
+        self._live[int(t.value)] = (x, out)
+        return int(t.value)
+
+    def result(self, ticket: int, timeout: float = 0.0):
+        st = _lib.RequestStats()
+        status = _lib.lib().grgx_server_wait(self._h, ticket, float(timeout), ctypes.byref(st))
+        x, out = self._live.pop(ticket, (None, None))
+        _lib.check(status)
+        return out, {"submit_s": st.submit_s, "start_s": st.start_s, "done_s": st.done_s,
+                     "latency_s": st.done_s - st.submit_s, "batch_requests": int(st.batch_requests),
+                     "batch_rows": int(st.batch_rows)}
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            _lib.lib().grgx_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

@@ -1,0 +1,116 @@
+// grgx_matmul_batch: coalescing requests of different K into shared traversals.
+//
+// Requests with the same direction and dtype are stacked row-wise (their K x cols inputs one
+// under the other) into a single input of K_total rows, multiplied once, and the K_total x
+// out_cols product is split back into the requests' outputs.  A traversal's cost is one pass
+// over the edge ids plus K_total row gathers per edge, so stacking small-K requests shares the
+// edge stream, the level launches and the vector lanes a narrow request would leave idle.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "grgx_internal.h"
+
+namespace grgx {
+
+void matmul_impl(grgx_graph* g, int dtype, const void* input, uint64_t in_cols, uint64_t rows, int direction,
+                 void* output, uint64_t output_size, int emit_all, int by_indiv, const void* init, int init_kind,
+                 void* miss, uint32_t flags, void* stream);
+
+namespace {
+
+#define BATCH_CUDA(call)                                                                             \
+    do {                                                                                            \
+        cudaError_t e__ = (call);                                                                   \
+        if (e__ != cudaSuccess)                                                                     \
+            throw Error(e__ == cudaErrorMemoryAllocation ? GRGX_ERR_OUT_OF_MEMORY : GRGX_ERR_CUDA,  \
+                        std::string(#call) + ": " + cudaGetErrorString(e__));                        \
+    } while (0)
+
+size_t elem_bytes(int dtype) {
+    switch (dtype) {
+    case GRGX_F64: case GRGX_I64: case GRGX_U64: return 8;
+    case GRGX_F32: case GRGX_I32: case GRGX_U32: return 4;
+    case GRGX_I16: case GRGX_U16: return 2;
+    default: return 1;
+    }
+}
+
+}  // namespace
+
+// Default stacking width: the widest row one sweep tile covers (128 four-byte or 64 eight-byte
+// columns), where the per-column cost of a traversal has levelled off.
+uint64_t default_batch_cols(int dtype) { return elem_bytes(dtype) >= 8 ? 64 : 128; }
+
+void matmul_batch_impl(grgx_graph* g, const grgx_request* reqs, uint64_t n, uint64_t maxCols, uint32_t flags,
+                       void* stream) {
+    GRGX_CHECK(n == 0 || reqs != nullptr, GRGX_ERR_API_MISUSE, "null argument");
+    const HostGraph& hg = *g->host;
+    const bool dev = (flags & GRGX_FLAG_DEVICE_POINTERS) != 0;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    // group by (direction, dtype), keeping submission order inside a group
+    std::map<std::pair<int, int>, std::vector<uint64_t>> groups;
+    for (uint64_t i = 0; i < n; i++) {
+        const grgx_request& r = reqs[i];
+        GRGX_CHECK(r.input && r.output && r.rows > 0, GRGX_ERR_API_MISUSE, "matmul() requires non-zero dimensions.");
+        GRGX_CHECK(r.direction == GRGX_DIRECTION_DOWN || r.direction == GRGX_DIRECTION_UP, GRGX_ERR_API_MISUSE,
+                   "Invalid traversal direction");
+        GRGX_CHECK(r.dtype >= GRGX_F64 && r.dtype <= GRGX_BOOL, GRGX_ERR_API_MISUSE, "Unsupported dtype");
+        groups[{static_cast<int>(r.direction), static_cast<int>(r.dtype)}].push_back(i);
+    }
+    const uint32_t passFlags = (flags & (GRGX_FLAG_F32_PLAIN | GRGX_FLAG_F64_NATIVE)) | GRGX_FLAG_DEVICE_POINTERS |
+                               GRGX_FLAG_OVERWRITE;
+    for (auto& kv : groups) {
+        const int direction = kv.first.first, dtype = kv.first.second;
+        const uint64_t cols = (direction == GRGX_DIRECTION_UP) ? hg.num_samples : hg.num_mutations;
+        const uint64_t outCols = (direction == GRGX_DIRECTION_UP) ? hg.num_mutations : hg.num_samples;
+        const size_t es = elem_bytes(dtype);
+        const uint64_t width = maxCols ? maxCols : default_batch_cols(dtype);
+        const std::vector<uint64_t>& idx = kv.second;
+        size_t i = 0;
+        while (i < idx.size()) {
+            // greedy: stack requests in order while the stacked rows fit `width` (a wider request
+            // runs alone)
+            uint64_t rowsTotal = reqs[idx[i]].rows;
+            size_t j = i + 1;
+            while (j < idx.size() && rowsTotal + reqs[idx[j]].rows <= width) rowsTotal += reqs[idx[j++]].rows;
+            if (j == i + 1) {
+                const grgx_request& r = reqs[idx[i]];
+                matmul_impl(g, dtype, r.input, cols, r.rows, direction, r.output, r.rows * outCols, 0, 0, nullptr,
+                            GRGX_INIT_ZERO, nullptr, (flags & ~GRGX_FLAG_SYNC) | GRGX_FLAG_OVERWRITE, stream);
+                i = j;
+                continue;
+            }
+            void* in = nullptr;
+            void* out = nullptr;
+            BATCH_CUDA(cudaMallocAsync(&in, rowsTotal * cols * es, s));
+            BATCH_CUDA(cudaMallocAsync(&out, rowsTotal * outCols * es, s));
+            uint64_t row = 0;
+            for (size_t k = i; k < j; k++) {
+                const grgx_request& r = reqs[idx[k]];
+                BATCH_CUDA(cudaMemcpyAsync(static_cast<char*>(in) + row * cols * es, r.input, r.rows * cols * es,
+                                           dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+                row += r.rows;
+            }
+            matmul_impl(g, dtype, in, cols, rowsTotal, direction, out, rowsTotal * outCols, 0, 0, nullptr,
+                        GRGX_INIT_ZERO, nullptr, passFlags, stream);
+            row = 0;
+            for (size_t k = i; k < j; k++) {
+                const grgx_request& r = reqs[idx[k]];
+                BATCH_CUDA(cudaMemcpyAsync(r.output, static_cast<char*>(out) + row * outCols * es,
+                                           r.rows * outCols * es,
+                                           dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
+                row += r.rows;
+            }
+            BATCH_CUDA(cudaFreeAsync(in, s));
+            BATCH_CUDA(cudaFreeAsync(out, s));
+            i = j;
+        }
+    }
+    if (!dev || (flags & GRGX_FLAG_SYNC)) BATCH_CUDA(cudaStreamSynchronize(s));
+}
+
+}  // namespace grgx

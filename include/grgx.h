@@ -133,6 +133,57 @@ grgx_status grgx_matmul(grgx_graph* g, grgx_dtype dtype, const void* input, uint
                         int emit_all_nodes, int by_individual, const void* init, grgx_init init_kind, void* miss,
                         uint32_t flags, void* stream);
 
+/* One request of a batch or of the server: the plain product (no init, miss, emit_all_nodes or
+ * by_individual) of `rows` x cols `input` in `direction`, written to `output` (rows x out_cols,
+ * overwritten).  Host or device memory as the call's flags say. */
+typedef struct {
+    grgx_dtype dtype;
+    grgx_direction direction;
+    uint64_t rows;
+    const void* input;
+    void* output;
+} grgx_request;
+
+/* No counterpart in the reference (its callers loop over matMul calls).  Runs `n` requests on
+ * one graph with as few traversals as possible: requests of the same direction and dtype are
+ * stacked row-wise into traversals of at most `max_cols` columns (0 = a default sized for the
+ * sweep's vector width), so the edge stream and the launches are shared.  Each request's
+ * result equals its own grgx_matmul result (bit-exact for integers; float sums may round
+ * differently because the stacked row is wider).  Flags as grgx_matmul
+ * (GRGX_FLAG_DEVICE_POINTERS, GRGX_FLAG_F32_PLAIN, GRGX_FLAG_F64_NATIVE). */
+grgx_status grgx_matmul_batch(grgx_graph* g, const grgx_request* requests, uint64_t n, uint64_t max_cols,
+                              uint32_t flags, void* stream);
+
+/* ---- serving: resident graphs, continuous batching ------------------------------------------
+ * No counterpart in the reference.  A server owns `workers` threads, each with its own CUDA
+ * stream on the device current at creation.  Submitted requests queue; whenever a worker is
+ * free it takes the oldest request plus every queued request for the same graph, direction and
+ * dtype that fits `max_cols` stacked rows, admits the batch only if its estimated device
+ * memory fits beside the batches in flight (`memory_budget`, 0 = 90% of the free memory at
+ * creation), runs it as one traversal and hands each request its own rows.  Requests that
+ * arrive while batches run are picked up as workers free up, so work from several batches
+ * overlaps on the device.  Request buffers are host memory and must stay valid until
+ * grgx_server_wait returns for their ticket. */
+typedef struct grgx_server grgx_server;
+
+typedef struct {
+    double submit_s; /* seconds since server creation */
+    double start_s;  /* batch launch */
+    double done_s;   /* result written */
+    uint64_t batch_requests;
+    uint64_t batch_rows;
+} grgx_request_stats;
+
+grgx_status grgx_server_create(uint32_t workers, uint64_t memory_budget, uint64_t max_cols, grgx_server** out);
+/* The graph must outlive the server; it is uploaded to the server's device here. */
+grgx_status grgx_server_add_graph(grgx_server* s, grgx_graph* g, uint32_t* graph_id);
+grgx_status grgx_server_submit(grgx_server* s, uint32_t graph_id, const grgx_request* request, uint64_t* ticket);
+/* Blocks until the request is done (or `timeout_s` passes: GRGX_ERR_TIMEOUT); returns the
+ * request's own status and fills `stats` (may be NULL).  A ticket can be waited for once. */
+grgx_status grgx_server_wait(grgx_server* s, uint64_t ticket, double timeout_s, grgx_request_stats* stats);
+/* Stops the workers after the batches in flight; queued requests fail with GRGX_ERR_TIMEOUT. */
+void grgx_server_destroy(grgx_server* s);
+
 /* Size of the static device scratch behind grgx_matmul_noalloc (64 MiB on every GPU that loads
  * the library, held until the process exits). */
 #define GRGX_NOALLOC_SCRATCH_BYTES (64ull << 20)
