@@ -49,6 +49,9 @@ def parse_args():
                     help="restrict the step to dtype:K:dir entries, e.g. float32:64:UP,int32:1:DOWN")
     ap.add_argument("--breakdown", action="store_true",
                     help="print per-matmul device times (3 calls each, CUDA events) instead of the JSON line")
+    ap.add_argument("--no-serve", action="store_true", help="skip the batched and served measurements")
+    ap.add_argument("--serve-rate", type=float, default=20.0, help="Poisson arrival rate (requests/s)")
+    ap.add_argument("--serve-seconds", type=float, default=5.0, help="arrival window of the served run")
     return ap.parse_args()
 
 
@@ -159,6 +162,94 @@ def cpu_baseline(args, combos, seconds_budget, threads=None):
             "sample": f"window-tree N={args.samples} M={sample_m} (E={E}); "
                       f"{'all' if time.perf_counter() - t_start <= seconds_budget else 'first'} workload combos; "
                       f"{total_units:.3g} edge*K in {total_t:.1f}s"}
+
+
+def batched_vs_plain(gx, torch, g, E, rng, n_req, kmax, label):
+    """Plain one-request-per-call against matmul_batch on the same requests (device inputs)."""
+    N, M = g.num_samples, g.num_mutations
+    reqs = []
+    for _ in range(n_req):
+        K = int(rng.integers(1, kmax + 1))
+        d = UP if rng.random() < 0.5 else DOWN
+        reqs.append((torch.from_numpy(rng.standard_normal((K, N if d == UP else M)).astype(np.float32)).cuda(), d))
+    units = sum(E * V.shape[0] for V, _ in reqs)
+    for _ in range(2):  # warm both paths (pool, plans)
+        gx.matmul(g, reqs[0][0], reqs[0][1])
+        gx.matmul_batch(g, reqs[:2])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for V, d in reqs:
+        gx.matmul(g, V, d)
+    torch.cuda.synchronize()
+    t_plain = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    gx.matmul_batch(g, reqs)
+    torch.cuda.synchronize()
+    t_batch = time.perf_counter() - t0
+    return {"mix": label, "requests": n_req, "plain_edgeK_per_s": units / t_plain,
+            "batched_edgeK_per_s": units / t_batch, "speedup": t_plain / t_batch}
+
+
+def served(gx, graphs, rate, seconds, rng):
+    """Poisson arrivals over resident graphs (K log-uniform in [1, 256], UP/DOWN and int32/float32
+    mixed), served by the continuous-batching server; against the same requests one per call."""
+    import threading
+
+    sizes = [(g.num_samples, g.num_mutations, g.num_edges) for g in graphs]
+    pools = {}
+    for gi, (N, M, _) in enumerate(sizes):
+        for d in (UP, DOWN):
+            cols = N if d == UP else M
+            pools[(gi, d, "int32")] = rng.integers(0, 2, size=(256, cols)).astype(np.int32)
+            pools[(gi, d, "float32")] = rng.standard_normal((256, cols)).astype(np.float32)
+    arrivals, t = [], 0.0
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t > seconds:
+            break
+        gi = 0 if rng.random() < 0.7 else 1
+        K = int(np.exp(rng.uniform(0.0, np.log(256.0))))
+        d = UP if rng.random() < 0.5 else DOWN
+        dt = "int32" if rng.random() < 0.5 else "float32"
+        arrivals.append((t, gi, d, pools[(gi, d, dt)][:K]))
+    units = sum(sizes[gi][2] * V.shape[0] for _, gi, _, V in arrivals)
+    lat = []
+    with gx.Server(workers=3) as srv:
+        ids = [srv.add_graph(g) for g in graphs]
+        srv.result(srv.submit(ids[0], pools[(0, UP, "int32")][:1], UP), timeout=120)  # warm
+        tickets = [None] * len(arrivals)
+
+        def producer():
+            t_start = time.perf_counter()
+            for i, (ta, gi, d, V) in enumerate(arrivals):
+                delay = ta - (time.perf_counter() - t_start)
+                if delay > 0:
+                    time.sleep(delay)
+                tickets[i] = srv.submit(ids[gi], V, d)
+
+        th = threading.Thread(target=producer)
+        t0 = time.perf_counter()
+        th.start()
+        batches = []
+        for i in range(len(arrivals)):
+            while tickets[i] is None:
+                time.sleep(0.0005)
+            _, st = srv.result(tickets[i], timeout=600)
+            lat.append(st["latency_s"])
+            batches.append(st["batch_requests"])
+        th.join()
+        t_served = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    for _, gi, d, V in arrivals:
+        gx.matmul(graphs[gi], V, d)
+    t_plain = time.perf_counter() - t0
+    lat_ms = np.array(lat) * 1e3
+    return {"arrival_rate_per_s": rate, "requests": len(arrivals), "graphs": [
+                {"samples": N, "mutations": M, "edges": E} for N, M, E in sizes],
+            "p50_ms": float(np.percentile(lat_ms, 50)), "p99_ms": float(np.percentile(lat_ms, 99)),
+            "served_edgeK_per_s": units / t_served, "plain_sequential_edgeK_per_s": units / t_plain,
+            "mean_batch_requests": float(np.mean(batches)),
+            "note": "served throughput is bounded by the offered load; plain = the same requests one per call"}
 
 
 def run_reference(args):
@@ -279,7 +370,9 @@ def main():
     achieved = abytes / (sweep_ms / 1000.0) / 1e9
     traffic = None
     tfile = ROOT / "profiles" / "sweep_traffic.json"
-    if tfile.exists():
+    default_step = (not args.only and args.samples == 200_000 and args.mutations == 1_000_000
+                    and args.ks == "1,8,32,64" and args.dtypes == "int32,float32,float64")
+    if tfile.exists() and default_step:
         traffic = json.loads(tfile.read_text()).get("bytes_per_step")
 
     # end to end: host buffers through the C-ABI (copies inside the timed region)
@@ -295,6 +388,15 @@ def main():
         barrier()
         e2e_s = time.perf_counter() - t0
         e2e_value = units_per_step * e2e_steps * world / e2e_s
+
+    batched = serve = None
+    if rank == 0 and not args.no_serve:
+        rng2 = np.random.default_rng(11)
+        batched = [batched_vs_plain(gx, torch, g, stats["edges"], rng2, 48, 128, "K~U{1..128}, UP/DOWN 50/50, float32"),
+                   batched_vs_plain(gx, torch, g, stats["edges"], rng2, 48, 8, "K~U{1..8}, UP/DOWN 50/50, float32")]
+        g2 = gx.window_tree_grg(max(2, args.samples // 4), max(1, args.mutations * 3 // 10), seed=args.seed + 1)
+        g2.upload()
+        serve = served(gx, [g, g2], args.serve_rate, args.serve_seconds, rng2)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -312,6 +414,10 @@ def main():
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
+                         "traffic_unit": "DRAM bytes per step, summed over the step's sweep launches (ncu, "
+                                         "profiles/sweep_traffic.json)",
+                         "l2_resident": True if traffic is None else traffic < 0.5 * abytes / args.steps,
+                         "dram_frac": None if traffic is None else traffic / (sweep_ms / args.steps / 1e3) / 1e9 / peak,
                          "compulsory_frac": compulsory / (sweep_ms / 1000.0) / 1e9 / peak,
                          "kernel": "grgx::sweep_kernel", "sweep_ms_per_step": sweep_ms / args.steps,
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback 6800"},
@@ -319,6 +425,8 @@ def main():
             "gpu_launches": launches,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "cpu_baseline": cpu,
+            "batched_vs_plain": batched,
+            "served": serve,
             "setup_s": {"generate": t_gen, "plan_upload": t_up},
         }
         print(json.dumps(line), flush=True)

@@ -126,6 +126,11 @@ class GRG:
         _lib.check(_lib.lib().grgx_graph_export(self._h, *(a.ctypes.data for a in out.values())))
         return out
 
+    def subset_mutations(self, mutation_ids) -> "GRG":
+        """The sub-GRG of the given mutations (saveGRGSubset by mutations, serialize.h:147-166)."""
+        ids = np.ascontiguousarray(mutation_ids, dtype=np.uint32)
+        return _new(_lib.lib().grgx_graph_subset, self._h, ids.ctypes.data if len(ids) else None, len(ids))
+
     def get_down_edges(self, node: int) -> list:
         a = self._cached_arrays()
         return a["down_adj"][a["down_off"][node]:a["down_off"][node + 1]].tolist()

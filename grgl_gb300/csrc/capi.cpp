@@ -133,6 +133,71 @@ grgx_status grgx_graph_generate(uint64_t num_samples, uint64_t num_mutations, ui
     });
 }
 
+grgx_status grgx_graph_subset(const grgx_graph* g, const uint32_t* mutation_ids, uint64_t n, grgx_graph** out) {
+    return guarded([&] {
+        GRGX_CHECK(g && out && (n == 0 || mutation_ids), GRGX_ERR_API_MISUSE, "null argument");
+        const HostGraph& h = *g->host;
+        std::vector<uint8_t> keep(h.num_nodes, 0);
+        for (uint64_t s = 0; s < h.num_samples; s++) keep[s] = 1;
+        std::vector<uint32_t> stack;
+        auto seed = [&](uint32_t v) {
+            if (v != INVALID_NODE && !keep[v]) {
+                keep[v] = 1;
+                stack.push_back(v);
+            }
+        };
+        for (uint64_t i = 0; i < n; i++) {
+            GRGX_CHECK(mutation_ids[i] < h.num_mutations, GRGX_ERR_API_MISUSE,
+                       "Invalid MutationID: " + std::to_string(mutation_ids[i]));
+            seed(h.mut_node[mutation_ids[i]]);
+            if (!h.miss_node.empty()) seed(h.miss_node[mutation_ids[i]]);
+        }
+        while (!stack.empty()) {
+            const uint32_t v = stack.back();
+            stack.pop_back();
+            for (uint64_t e = h.down_off[v]; e < h.down_off[v + 1]; e++) seed(h.down_adj[e]);
+        }
+        std::vector<uint32_t> remap(h.num_nodes, INVALID_NODE);
+        uint64_t cnt = 0;
+        for (uint64_t v = 0; v < h.num_nodes; v++)
+            if (keep[v]) remap[v] = static_cast<uint32_t>(cnt++);
+        auto sub = std::make_unique<HostGraph>();
+        sub->num_nodes = cnt;
+        sub->num_samples = h.num_samples;
+        sub->ploidy = h.ploidy;
+        sub->phased = h.phased;
+        sub->num_mutations = n;
+        sub->down_off.assign(1, 0);
+        for (uint64_t v = 0; v < h.num_nodes; v++) {
+            if (!keep[v]) continue;
+            for (uint64_t e = h.down_off[v]; e < h.down_off[v + 1]; e++) sub->down_adj.push_back(remap[h.down_adj[e]]);
+            sub->down_off.push_back(sub->down_adj.size());
+        }
+        sub->mut_node.resize(n);
+        for (uint64_t i = 0; i < n; i++) {
+            const uint32_t v = h.mut_node[mutation_ids[i]];
+            sub->mut_node[i] = (v == INVALID_NODE) ? INVALID_NODE : remap[v];
+        }
+        if (!h.miss_node.empty()) {
+            sub->miss_node.resize(n);
+            for (uint64_t i = 0; i < n; i++) {
+                const uint32_t v = h.miss_node[mutation_ids[i]];
+                sub->miss_node[i] = (v == INVALID_NODE) ? INVALID_NODE : remap[v];
+            }
+        }
+        if (!h.coals.empty()) {
+            for (uint64_t v = h.num_samples; v < h.num_nodes; v++)
+                if (keep[v]) sub->coals.push_back(v - h.num_samples < h.coals.size() ? h.coals[v - h.num_samples]
+                                                                                    : COAL_NOT_SET);
+        }
+        if (!h.mut_pos.empty())
+            for (uint64_t i = 0; i < n; i++) sub->mut_pos.push_back(h.mut_pos[mutation_ids[i]]);
+        auto gg = new grgx_graph();
+        gg->host = std::move(sub);
+        *out = gg;
+    });
+}
+
 void grgx_graph_destroy(grgx_graph* g) {
     if (!g) return;
     try {

@@ -111,6 +111,13 @@ grgx_status grgx_graph_info_get(const grgx_graph* g, grgx_graph_info* out);
 grgx_status grgx_graph_export(const grgx_graph* g, uint64_t* down_off, uint32_t* down_adj, uint32_t* mut_node,
                               uint32_t* miss_node, uint32_t* coals);
 
+/* Replaces grgl::saveGRGSubset(..., DIRECTION_DOWN, seedList, ...) (include/grgl/serialize.h:147-166)
+ * without the file round trip: a new graph holding the listed mutations (renumbered in list
+ * order), every sample (same ids), and the nodes reachable downward from the mutations' (and
+ * their missingness) nodes, in their original relative order.  Range shards of one graph have
+ * disjoint mutations; their UP outputs concatenate and their DOWN outputs sum. */
+grgx_status grgx_graph_subset(const grgx_graph* g, const uint32_t* mutation_ids, uint64_t n, grgx_graph** out);
+
 /* Builds the level plan and copies it to the current device (done implicitly by the first
  * grgx_matmul; explicit here so callers can keep it out of timed regions). */
 grgx_status grgx_graph_upload(grgx_graph* g);
