@@ -8,10 +8,11 @@ The compute runs in libgrgx.so (hand-written sm_103a CUDA kernels behind a C ABI
 include/grgx.h); there is no CPU implementation in this package.
 """
 from .api import (COAL_COUNT_NOT_SET, DOWN, GRG, INVALID_NODE, UP, Server, TraversalDirection, dot_product, from_csr,
-                  from_pygrgl, last_timing, load_immutable_grg, matmul, matmul_batch, set_timing, window_tree_grg)
+                  from_pygrgl, last_timing, load_immutable_grg, matmul, matmul_batch, matmul_standardized, set_timing,
+                  window_tree_grg)
 
 __all__ = [
     "COAL_COUNT_NOT_SET", "DOWN", "GRG", "INVALID_NODE", "UP", "TraversalDirection", "dot_product", "from_csr",
     "from_pygrgl", "last_timing", "load_immutable_grg", "matmul", "matmul_batch", "set_timing", "window_tree_grg",
-    "Server",
+    "Server", "matmul_standardized",
 ]

@@ -350,6 +350,37 @@ def last_timing() -> dict:
             "alg_bytes": int(t.alg_bytes)}
 
 
+def matmul_standardized(grg: GRG, input, direction, *, f32_compensated: bool = True, f64_native: bool = False):
+    """Product with the standardized genotype matrix Z = (X - mu) / sigma (haploid p_j, sigma_j =
+    sqrt(p_j(1-p_j)), zero-variance columns masked): ``V Z`` for UP (V: K x N), ``V Z^T`` for DOWN
+    (V: K x M).  float32/float64; the reductions it divides by are float64 on the GPU."""
+    direction = TraversalDirection(int(direction))
+    flags = _flags(f32_compensated, f64_native)
+    rows_out = grg.num_mutations if direction == UP else grg.num_samples
+    if _is_torch_cuda(input):
+        import torch
+
+        x = input.contiguous()
+        _check(x.dim() == 2 and x.dtype in (torch.float32, torch.float64),
+               "standardized products take 2-D float32 or float64 input")
+        out = torch.empty((x.shape[0], rows_out), dtype=x.dtype, device=x.device)
+        code = 0 if x.dtype == torch.float64 else 1
+        stream = torch.cuda.current_stream(x.device).cuda_stream
+        _lib.check(_lib.lib().grgx_matmul_standardized(grg._h, code, x.data_ptr(), x.shape[1], x.shape[0],
+                                                       int(direction), out.data_ptr(), out.numel(),
+                                                       flags | _lib.FLAG_DEVICE_POINTERS, stream))
+        return out
+    _check(isinstance(input, np.ndarray), f"Unsupported numpy dtype: {np.asarray(input).dtype}")
+    x = np.ascontiguousarray(input)
+    _check(x.ndim == 2, "matmul() only support two dimensional numpy arrays as input.")
+    _check(x.dtype in (np.float32, np.float64), "standardized products take float32 or float64 input")
+    out = np.empty((x.shape[0], rows_out), dtype=x.dtype)
+    _lib.check(_lib.lib().grgx_matmul_standardized(grg._h, 0 if x.dtype == np.float64 else 1, x.ctypes.data,
+                                                   x.shape[1], x.shape[0], int(direction), out.ctypes.data,
+                                                   out.size, flags, None))
+    return out
+
+
 # ---- batching and serving ----------------------------------------------------------------------
 
 

@@ -18,6 +18,8 @@ void matmul_noalloc_impl(grgx_graph* g, int dtype, const void* input, uint64_t i
                          void* output, uint64_t output_size, void* stream);
 void matmul_batch_impl(grgx_graph* g, const grgx_request* reqs, uint64_t n, uint64_t maxCols, uint32_t flags,
                        void* stream);
+void matmul_standardized_impl(grgx_graph* g, int dtype, const void* input, uint64_t in_cols, uint64_t rows,
+                              int direction, void* output, uint64_t output_size, uint32_t flags, void* stream);
 
 namespace {
 thread_local std::string t_error;
@@ -261,6 +263,16 @@ grgx_status grgx_matmul(grgx_graph* g, grgx_dtype dtype, const void* input, uint
         GRGX_CHECK(g && input && output, GRGX_ERR_API_MISUSE, "null argument");
         matmul_impl(g, dtype, input, input_cols, input_rows, direction, output, output_size, emit_all_nodes,
                     by_individual, init, init_kind, miss, flags, stream);
+    });
+}
+
+grgx_status grgx_matmul_standardized(grgx_graph* g, grgx_dtype dtype, const void* input, uint64_t input_cols,
+                                     uint64_t input_rows, grgx_direction direction, void* output,
+                                     uint64_t output_size, uint32_t flags, void* stream) {
+    return guarded([&] {
+        GRGX_CHECK(g && input && output, GRGX_ERR_API_MISUSE, "null argument");
+        matmul_standardized_impl(g, dtype, input, input_cols, input_rows, direction, output, output_size, flags,
+                                 stream);
     });
 }
 

@@ -42,6 +42,8 @@ struct DevicePlan {
     bool has_coals = false;
     bool has_miss = false;
     double xtx_max = 0.0;  // largest XTX init value (2 * coalescences)
+    double* freq = nullptr;       // allele frequency per mutation (standardized products)
+    double* inv_sigma = nullptr;  // 1/sqrt(p(1-p)) per mutation, 0 where p(1-p) == 0
     std::vector<void*> allocs;
 };
 

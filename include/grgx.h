@@ -140,6 +140,20 @@ grgx_status grgx_matmul(grgx_graph* g, grgx_dtype dtype, const void* input, uint
                         int emit_all_nodes, int by_individual, const void* init, grgx_init init_kind, void* miss,
                         uint32_t flags, void* stream);
 
+/* No counterpart in the reference (the operator grapp's standardized LinearOperators apply on top
+ * of GRGL's matmul; grapp is not part of GRGL).  Products with the standardized genotype matrix
+ * Z (N x M), Z[i, j] = (X[i, j] - mu_j) / sigma_j, mu_j = p_j = count_j / N, sigma_j =
+ * sqrt(p_j (1 - p_j)) (haploid), columns with sigma_j = 0 set to zero:
+ *   UP:   out = V Z   = ((V X) - (V 1) mu^T) / sigma        (V: K x N, out: K x M)
+ *   DOWN: out = V Z^T = X (V / sigma)^T - 1 (mu^T (V / sigma)^T)   (V: K x M, out: K x N)
+ * The products with X run on the sweep in the input's dtype (float32 compensated or float64);
+ * the allele frequencies are an exact int32 UP product computed once per graph, and the row
+ * sums V 1 and mu^T (V / sigma) are float64 reductions on the device.  float32/float64 only;
+ * `flags` as grgx_matmul (host or device pointers); the output is overwritten. */
+grgx_status grgx_matmul_standardized(grgx_graph* g, grgx_dtype dtype, const void* input, uint64_t input_cols,
+                                     uint64_t input_rows, grgx_direction direction, void* output,
+                                     uint64_t output_size, uint32_t flags, void* stream);
+
 /* One request of a batch or of the server: the plain product (no init, miss, emit_all_nodes or
  * by_individual) of `rows` x cols `input` in `direction`, written to `output` (rows x out_cols,
  * overwritten).  Host or device memory as the call's flags say. */

@@ -305,3 +305,23 @@ def read_grg(path) -> OracleGraph:
         pos += 4 * nmut
     return OracleGraph(num_samples=nsamp, ploidy=ploidy, down_off=off, down_adj=np.array(adj, dtype=np.uint32),
                        mut_node=mut_node, miss_node=miss, coals=coals)
+
+
+def standardized(g: OracleGraph, V: np.ndarray, direction: int, return_scale: bool = False):
+    """Float64 products with Z = (X - mu) / sigma from the dense genotype matrix (small graphs only).
+
+    mu_j = count_j / N (haploid), sigma_j = sqrt(mu_j (1 - mu_j)), zero-variance columns set to 0:
+    UP -> V @ Z, DOWN -> V @ Z.T.  With return_scale, also |V| @ |Z| (the magnitude the tolerance
+    is relative to)."""
+    X = g.dense_X().astype(np.float64)
+    N = X.shape[0]
+    mu = X.sum(axis=0) / N
+    var = mu * (1.0 - mu)
+    inv = np.where(var > 0, 1.0 / np.sqrt(np.where(var > 0, var, 1.0)), 0.0)
+    Z = (X - mu[None, :]) * inv[None, :]
+    V64 = V.astype(np.float64)
+    out = V64 @ Z if int(direction) == UP else V64 @ Z.T
+    if not return_scale:
+        return out
+    A = np.abs(Z)
+    return out, (np.abs(V64) @ A if int(direction) == UP else np.abs(V64) @ A.T)
