@@ -311,8 +311,9 @@ def standardized(g: OracleGraph, V: np.ndarray, direction: int, return_scale: bo
     """Float64 products with Z = (X - mu) / sigma from the dense genotype matrix (small graphs only).
 
     mu_j = count_j / N (haploid), sigma_j = sqrt(mu_j (1 - mu_j)), zero-variance columns set to 0:
-    UP -> V @ Z, DOWN -> V @ Z.T.  With return_scale, also |V| @ |Z| (the magnitude the tolerance
-    is relative to)."""
+    UP -> V @ Z, DOWN -> V @ Z.T.  With return_scale, also the magnitude of the terms the
+    algorithm combines (|V| X + |V 1| mu) / sigma for UP, |W| X^T + |W mu| for DOWN: the scale the
+    tolerance is relative to."""
     X = g.dense_X().astype(np.float64)
     N = X.shape[0]
     mu = X.sum(axis=0) / N
@@ -323,5 +324,12 @@ def standardized(g: OracleGraph, V: np.ndarray, direction: int, return_scale: bo
     out = V64 @ Z if int(direction) == UP else V64 @ Z.T
     if not return_scale:
         return out
-    A = np.abs(Z)
-    return out, (np.abs(V64) @ A if int(direction) == UP else np.abs(V64) @ A.T)
+    # The algorithm combines V X with the correction (V 1) mu^T (UP), or X W^T with 1 (mu^T W^T)
+    # (DOWN, W = V / sigma); its rounding is relative to the magnitudes of those terms.
+    aV = np.abs(V64)
+    if int(direction) == UP:
+        scale = ((aV @ X) + np.abs(V64.sum(axis=1))[:, None] * mu[None, :]) * inv[None, :]
+    else:
+        W = V64 * inv[None, :]
+        scale = np.abs(W) @ X.T + np.abs(W @ mu)[:, None]
+    return out, scale
