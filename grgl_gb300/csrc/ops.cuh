@@ -129,13 +129,14 @@ struct AddF32C {
 
 // Float64 on GB300 without the FP64 pipe in the inner loop.  Node values are stored as a
 // float pair (hi + lo, 48 significant bits) of the value scaled by 2^-e_k per input row k, so
-// each row's largest input sits in [1, 2) and every sum stays well inside float range.  Edge
-// sums run in float-float: TwoSum of the high parts, the rounding error and the low parts
-// folded into lo, then renormalised (the "sloppy" double-word addition; its error is at most a
-// few u^2 (|a| + |b|), u = 2^-24).  Every 32 additions the run is folded into a double, so a
-// run's error is bounded by ~32 * 4u^2 * sum|x| ~ 5e-13 of the terms' magnitudes and the
-// double chain adds the usual 1.1e-16 per fold.  `p` keeps the plain float sum of the high
-// parts, which carries IEEE inf/nan through exactly when an input is not finite.
+// each row's largest input sits in [2^60, 2^61) and every sum stays well inside float range.
+// Edge sums run in float-float: each addition takes the TwoSum error of the high parts and the
+// incoming low part into lo (hi stays the plain float sum); every 4 additions the pair is
+// renormalised (FastTwoSum), and every 32 additions the run is folded into a double.  A run's
+// error is then a few u^2 (u = 2^-24) per renormalised period -- ~8 * (16 + 1) u^2 sum|x| ~ 5e-13
+// of the terms' magnitudes over 32 additions -- and the double chain adds 1.1e-16 per fold.
+// `p` keeps the plain float sum of the high parts, which carries IEEE inf/nan through exactly
+// when an input is not finite.
 struct alignas(8) DF {
     float hi, lo;
 };
@@ -149,6 +150,7 @@ struct AddF64S {
     using S = DF;
     using A = F64Run;
     static __device__ __forceinline__ A zero() { return {0.0, 0.0f, 0.0f, 0.0f, 0.0f}; }
+    // normalised float-float addition (merges of partial sums)
     static __device__ __forceinline__ void run_add(float& hi, float& lo, float xh, float xl) {
         const float s = __fadd_rn(hi, xh);
         const float bb = __fsub_rn(s, hi);
@@ -157,9 +159,19 @@ struct AddF64S {
         hi = __fadd_rn(s, e);
         lo = __fsub_rn(e, __fsub_rn(hi, s));
     }
+    // one edge: hi keeps the plain sum, lo collects the exact error and the low part
     static __device__ __forceinline__ void add(A& a, S x) {
-        run_add(a.hi, a.lo, x.hi, x.lo);
+        const float s = __fadd_rn(a.hi, x.hi);
+        const float bb = __fsub_rn(s, a.hi);
+        const float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(x.hi, bb));
+        a.lo = __fadd_rn(a.lo, __fadd_rn(e, x.lo));
+        a.hi = s;
         a.p = __fadd_rn(a.p, x.hi);
+    }
+    static __device__ __forceinline__ void settle(A& a) {
+        const float h = __fadd_rn(a.hi, a.lo);
+        a.lo = __fsub_rn(a.lo, __fsub_rn(h, a.hi));
+        a.hi = h;
     }
     static __device__ __forceinline__ double run_value(const A& a) {
         return isfinite(a.p) ? (static_cast<double>(a.hi) + static_cast<double>(a.lo)) : static_cast<double>(a.p);
@@ -211,71 +223,6 @@ struct AddF64S {
     static __device__ __forceinline__ S finish(const A& a) { return split(a.acc + run_value(a)); }
     static __device__ __forceinline__ S finish_onto(S base, const A& a) {
         return split(value(base) + (a.acc + run_value(a)));
-    }
-};
-
-// ---- packed float2 arithmetic (Blackwell FADD2 / FFMA2) ---------------------------------------
-// Two float additions per instruction; a - b is formed as fma(b, -1, a), which is exact before
-// the single rounding, so every operation rounds exactly like the scalar __fadd_rn/__fsub_rn.
-__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
-__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.0f, -1.0f), a); }
-
-// acc[i] += v[i] for a lane's VW columns; the compensated operators use packed pairs.
-template <class Op, int VW> struct VecAdd {
-    static __device__ __forceinline__ void add(typename Op::A* acc, const typename Op::S* v) {
-#pragma unroll
-        for (int i = 0; i < VW; i++) Op::add(acc[i], v[i]);
-    }
-};
-
-template <int VW> struct VecAdd<AddF32C, VW> {
-    static __device__ __forceinline__ void add(F32Pair* acc, const float* v) {
-        if constexpr (VW % 2 == 0) {
-#pragma unroll
-            for (int j = 0; j < VW; j += 2) {
-                const float2 a = make_float2(acc[j].hi, acc[j + 1].hi);
-                const float2 b = make_float2(v[j], v[j + 1]);
-                const float2 s = add2(a, b);
-                const float2 bb = sub2(s, a);
-                const float2 e = add2(sub2(a, sub2(s, bb)), sub2(b, bb));
-                const float2 lo = add2(make_float2(acc[j].lo, acc[j + 1].lo), e);
-                acc[j] = {s.x, lo.x};
-                acc[j + 1] = {s.y, lo.y};
-            }
-        } else {
-#pragma unroll
-            for (int i = 0; i < VW; i++) AddF32C::add(acc[i], v[i]);
-        }
-    }
-};
-
-template <int VW> struct VecAdd<AddF64S, VW> {
-    static __device__ __forceinline__ void add(F64Run* acc, const DF* v) {
-        if constexpr (VW % 2 == 0) {
-#pragma unroll
-            for (int j = 0; j < VW; j += 2) {
-                const float2 hi = make_float2(acc[j].hi, acc[j + 1].hi);
-                const float2 lo = make_float2(acc[j].lo, acc[j + 1].lo);
-                const float2 xh = make_float2(v[j].hi, v[j + 1].hi);
-                const float2 xl = make_float2(v[j].lo, v[j + 1].lo);
-                const float2 s = add2(hi, xh);
-                const float2 bb = sub2(s, hi);
-                float2 e = add2(sub2(hi, sub2(s, bb)), sub2(xh, bb));
-                e = add2(e, add2(lo, xl));
-                const float2 nh = add2(s, e);
-                const float2 nl = sub2(e, sub2(nh, s));
-                const float2 p = add2(make_float2(acc[j].p, acc[j + 1].p), xh);
-                acc[j].hi = nh.x;
-                acc[j + 1].hi = nh.y;
-                acc[j].lo = nl.x;
-                acc[j + 1].lo = nl.y;
-                acc[j].p = p.x;
-                acc[j + 1].p = p.y;
-            }
-        } else {
-#pragma unroll
-            for (int i = 0; i < VW; i++) AddF64S::add(acc[i], v[i]);
-        }
     }
 };
 

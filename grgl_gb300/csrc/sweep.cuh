@@ -15,8 +15,10 @@
 // ticket) adds them up in piece order, so results do not depend on scheduling.
 #pragma once
 #include <cstdint>
+#include <type_traits>
 
 #include "ops.cuh"
+#include "vecacc.cuh"
 
 namespace grgx {
 
@@ -69,18 +71,18 @@ template <typename S, int VW> __device__ __forceinline__ void ld_plain(const S* 
     for (int i = 0; i < VW; i++) v[i] = p[i];
 }
 
-// Sum of a register vector over the 32/G groups of the warp (every group gets the result).
-template <class Op, int VW, int G> __device__ __forceinline__ void group_allreduce(typename Op::A* x) {
+// Sum of a lane's accumulator over the 32/G groups of the warp (every group gets the result).
+template <class Op, int VW, int G> __device__ __forceinline__ void group_allreduce(VecAcc<Op, VW>& x) {
 #pragma unroll
     for (int m = G; m < 32; m <<= 1) {
-#pragma unroll
-        for (int i = 0; i < VW; i++) Op::merge(x[i], Op::shfl_xor(x[i], m));
+        const auto t = x.shfl_xor(m);
+        x.merge(t);
     }
 }
 
 template <class Op, int VW>
 __device__ __forceinline__ void write_row(const SweepParams<typename Op::S>& p, long long row, int col,
-                                          const typename Op::A* tot) {
+                                          const VecAcc<Op, VW>& tot) {
     using S = typename Op::S;
     const long long node = p.rows[row];
     S* d = p.dst + node * p.stride + col;
@@ -89,10 +91,10 @@ __device__ __forceinline__ void write_row(const SweepParams<typename Op::S>& p, 
         S base[VW];
         ld_plain<S, VW>(d, base);
 #pragma unroll
-        for (int i = 0; i < VW; i++) out[i] = Op::finish_onto(base[i], tot[i]);
+        for (int i = 0; i < VW; i++) out[i] = Op::finish_onto(base[i], tot.get(i));
     } else {
 #pragma unroll
-        for (int i = 0; i < VW; i++) out[i] = Op::finish(tot[i]);
+        for (int i = 0; i < VW; i++) out[i] = Op::finish(tot.get(i));
     }
     Vec<S, VW>::st(d, out);
 }
@@ -114,22 +116,20 @@ __device__ __forceinline__ F32Pair ld_cg(const F32Pair* p) {
     return {t.x, t.y};
 }
 
-// Accumulation operators may bound the length of their running chains (AddF64S keeps at most
-// 32 additions in its float-float run before folding it into a double); the kernel calls
-// Op::flush after every `flush_steps` steps, where a step gives each lane STEPS additions.
-template <class Op> struct FlushTraits {
-    static constexpr bool kFlush = false;
-    static __device__ __forceinline__ void flush(typename Op::A&) {}
+// Accumulators may bound their running chains: AddF64S renormalises its float pair every 4
+// additions (settle) and folds it into a double every 32 (flush).
+template <class Op> struct ChainTraits {
+    static constexpr bool kChains = false;
 };
-template <> struct FlushTraits<AddF64S> {
-    static constexpr bool kFlush = true;
-    static __device__ __forceinline__ void flush(F64Run& a) { AddF64S::flush(a); }
+template <> struct ChainTraits<AddF64S> {
+    static constexpr bool kChains = true;
 };
 
 template <class Op, int VW, int G>
 __device__ __forceinline__ void sweep_chunk(const SweepParams<typename Op::S>& p, long long c, int lane) {
     using S = typename Op::S;
     using A = typename Op::A;
+    using Acc = VecAcc<Op, VW>;
     constexpr int NG = 32 / G;  // groups per warp = edges per sub-step
     // gathers in flight per lane: 4 for 16-byte vectors, 8 for narrower ones
     constexpr int BATCH = (VW * sizeof(S) >= 16) ? 4 : 8;
@@ -137,6 +137,7 @@ __device__ __forceinline__ void sweep_chunk(const SweepParams<typename Op::S>& p
     constexpr int STEPS = UNR * G;                     // sub-steps per step (a multiple of BATCH)
     constexpr unsigned NGMASK = (NG == 32) ? 0xffffffffu : ((1u << NG) - 1u);
     constexpr int FLUSH_EVERY = (STEPS >= 32) ? 1 : 32 / STEPS;
+    constexpr bool kChains = ChainTraits<Op>::kChains;
 
     const int lg = lane / G;  // group
     const int li = lane % G;  // lane inside the group
@@ -147,9 +148,8 @@ __device__ __forceinline__ void sweep_chunk(const SweepParams<typename Op::S>& p
     const ChunkDev ch = p.chunks[c];
     const long long eEnd = p.chunks[c + 1].e0;
 
-    A acc[VW];
-#pragma unroll
-    for (int i = 0; i < VW; i++) acc[i] = Op::zero();
+    Acc acc;
+    acc.zero();
     long long cur = ch.r0;
     bool first = true;
     int nsteps = 0;
@@ -192,7 +192,8 @@ __device__ __forceinline__ void sweep_chunk(const SweepParams<typename Op::S>& p
                 const int t = t0 + u;
                 const int b = t / G, s = t % G;
                 const int j = s * NG + lg;
-                const uint32_t idx = __shfl_sync(FULL_MASK, raw[b], j) & 0x7fffffffu;
+                // with one lane per row (G == 1) each lane gathers the edge id it loaded itself
+                const uint32_t idx = ((G == 1) ? raw[b] : __shfl_sync(FULL_MASK, raw[b], j)) & 0x7fffffffu;
                 if (32 * b + j < left && colok) {
                     Vec<S, VW>::ld(p.src + (long long)idx * p.stride + col, v[u]);
                 } else {
@@ -203,7 +204,10 @@ __device__ __forceinline__ void sweep_chunk(const SweepParams<typename Op::S>& p
             if (anyHead == 0u) {
                 // no row starts in this step: every edge continues the current row
 #pragma unroll
-                for (int u = 0; u < BATCH; u++) VecAdd<Op, VW>::add(acc, v[u]);
+                for (int u = 0; u < BATCH; u++) {
+                    acc.add(v[u]);
+                    if (kChains && (u & 3) == 3) acc.settle();
+                }
                 continue;
             }
 #pragma unroll
@@ -212,55 +216,43 @@ __device__ __forceinline__ void sweep_chunk(const SweepParams<typename Op::S>& p
                 const int b = t / G, s = t % G;
                 const unsigned hs = (NG == 32) ? heads[b] : ((heads[b] >> (s * NG)) & NGMASK);
                 if (hs == 0u) {
-                    VecAdd<Op, VW>::add(acc, v[u]);
+                    acc.add(v[u]);
+                    if (kChains && (u & 3) == 3) acc.settle();
                     continue;
                 }
                 const int q = __popc(hs & upto);  // rows started at or before my edge
                 const int Q = __popc(hs);
                 // 1) the current row ends in this sub-step
-                A x[VW];
-#pragma unroll
-                for (int i = 0; i < VW; i++) {
-                    x[i] = acc[i];
-                    if (q == 0) Op::add(x[i], v[u][i]);
-                }
+                Acc x = acc;
+                if (q == 0) x.add(v[u]);
                 group_allreduce<Op, VW, G>(x);
                 if (cur >= ch.r0 && lg == 0 && colok) write_row<Op, VW>(p, cur, col, x);
                 // 2) rows that start and end inside this sub-step: segmented scan over groups
                 if (Q > 1) {
-                    A y[VW];
-#pragma unroll
-                    for (int i = 0; i < VW; i++) {
-                        y[i] = Op::zero();
-                        if (q >= 1) Op::add(y[i], v[u][i]);
-                    }
+                    Acc y;
+                    y.zero();
+                    if (q >= 1) y.add(v[u]);
 #pragma unroll
                     for (int d = 1; d < NG; d <<= 1) {
                         const int qu = __shfl_up_sync(FULL_MASK, q, d * G);
-#pragma unroll
-                        for (int i = 0; i < VW; i++) {
-                            const A tv = Op::shfl_up(y[i], d * G);
-                            if (lg >= d && qu == q) Op::merge(y[i], tv);
-                        }
+                        const auto tv = y.shfl_up(d * G);
+                        if (lg >= d && qu == q) y.merge(tv);
                     }
                     const int qn = __shfl_down_sync(FULL_MASK, q, G);
                     const bool tail = (lg == NG - 1) || (qn != q);
                     if (tail && q >= 1 && q < Q && colok) write_row<Op, VW>(p, cur + q, col, y);
                 }
                 // 3) the last row continues into the next sub-step
-#pragma unroll
-                for (int i = 0; i < VW; i++) {
-                    acc[i] = Op::zero();
-                    if (q == Q) Op::add(acc[i], v[u][i]);
-                }
+                acc.zero();
+                if (q == Q) acc.add(v[u]);
                 cur += Q;
             }
         }
-        if constexpr (FlushTraits<Op>::kFlush) {
+        if (kChains) {
             if (++nsteps == FLUSH_EVERY) {
                 nsteps = 0;
-#pragma unroll
-                for (int i = 0; i < VW; i++) FlushTraits<Op>::flush(acc[i]);
+                acc.settle();
+                acc.flush();
             }
         }
     }
@@ -276,7 +268,7 @@ __device__ __forceinline__ void sweep_chunk(const SweepParams<typename Op::S>& p
     A* part = reinterpret_cast<A*>(p.partials);
     if (lg == 0 && colok) {
 #pragma unroll
-        for (int i = 0; i < VW; i++) part[(hr.slot_base + piece) * p.stride + col + i] = acc[i];
+        for (int i = 0; i < VW; i++) part[(hr.slot_base + piece) * p.stride + col + i] = acc.get(i);
     }
     __threadfence();
     __syncwarp();
@@ -285,14 +277,13 @@ __device__ __forceinline__ void sweep_chunk(const SweepParams<typename Op::S>& p
     ticket = __shfl_sync(FULL_MASK, ticket, 0);
     if (ticket != (unsigned)hr.n_pieces - 1u) return;
     __threadfence();
-    A sum[VW];
-#pragma unroll
-    for (int i = 0; i < VW; i++) sum[i] = Op::zero();
+    Acc sum;
+    sum.zero();
     if (colok) {
         for (int pc = lg; pc < hr.n_pieces; pc += NG) {
             const A* src = part + (hr.slot_base + pc) * p.stride + col;
 #pragma unroll
-            for (int i = 0; i < VW; i++) Op::merge(sum[i], ld_cg(src + i));
+            for (int i = 0; i < VW; i++) sum.add_partial(i, ld_cg(src + i));
         }
     }
     group_allreduce<Op, VW, G>(sum);
@@ -303,7 +294,9 @@ __device__ __forceinline__ void sweep_chunk(const SweepParams<typename Op::S>& p
 // left, so long and short chunks balance across the SMs.
 // Blocks per SM the register budget is sized for (65536 / (256 * blocks) registers per thread).
 template <class Op, int VW, int G> struct SweepOccupancy {
-    static constexpr int kBlocks = 4;
+    // compensated float shapes with several 32-edge blocks per step hold more state per lane
+    static constexpr bool kWide = (std::is_same<Op, AddF32C>::value || std::is_same<Op, AddF64S>::value) && G <= 2 && VW >= 2;
+    static constexpr int kBlocks = kWide ? 3 : 4;
 };
 
 template <class Op, int VW, int G>

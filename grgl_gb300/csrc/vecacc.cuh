@@ -1,0 +1,234 @@
+// Per-lane accumulators for the VW columns a lane owns in the sweep.
+//
+// The generic VecAcc keeps one scalar accumulator per column.  The compensated float32 and the
+// float-pair float64 operators keep their state as float2 pairs of adjacent columns (structure
+// of arrays), so every addition is a packed FP32x2 instruction (FADD2, or FFMA2 with a -1
+// multiplier for an exact subtraction) on register pairs that need no repacking.
+#pragma once
+#include "ops.cuh"
+
+namespace grgx {
+
+// ---- packed float2 arithmetic (Blackwell FADD2 / FFMA2) --------------------------------------
+// Each operation rounds exactly like the scalar __fadd_rn / __fsub_rn of its component.
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.0f, -1.0f), a); }
+__device__ __forceinline__ float2 shfl_xor2(float2 a, int m) {
+    return make_float2(__shfl_xor_sync(FULL_MASK, a.x, m), __shfl_xor_sync(FULL_MASK, a.y, m));
+}
+__device__ __forceinline__ float2 shfl_up2(float2 a, int d) {
+    return make_float2(__shfl_up_sync(FULL_MASK, a.x, d), __shfl_up_sync(FULL_MASK, a.y, d));
+}
+__device__ __forceinline__ float lane_of(float2 a, int i) { return (i & 1) ? a.y : a.x; }
+
+// TwoSum on pairs: s = a + b rounded, e = exact error.
+__device__ __forceinline__ void two_sum2(float2 a, float2 b, float2& s, float2& e) {
+    s = add2(a, b);
+    const float2 bb = sub2(s, a);
+    e = add2(sub2(a, sub2(s, bb)), sub2(b, bb));
+}
+
+template <class Op, int VW> struct VecAcc {
+    using S = typename Op::S;
+    using A = typename Op::A;
+    A a[VW];
+    __device__ __forceinline__ void zero() {
+#pragma unroll
+        for (int i = 0; i < VW; i++) a[i] = Op::zero();
+    }
+    __device__ __forceinline__ void add(const S* v) {
+#pragma unroll
+        for (int i = 0; i < VW; i++) Op::add(a[i], v[i]);
+    }
+    __device__ __forceinline__ void merge(const VecAcc& o) {
+#pragma unroll
+        for (int i = 0; i < VW; i++) Op::merge(a[i], o.a[i]);
+    }
+    __device__ __forceinline__ VecAcc shfl_xor(int m) const {
+        VecAcc r;
+#pragma unroll
+        for (int i = 0; i < VW; i++) r.a[i] = Op::shfl_xor(a[i], m);
+        return r;
+    }
+    __device__ __forceinline__ VecAcc shfl_up(int d) const {
+        VecAcc r;
+#pragma unroll
+        for (int i = 0; i < VW; i++) r.a[i] = Op::shfl_up(a[i], d);
+        return r;
+    }
+    __device__ __forceinline__ A get(int i) const { return a[i]; }
+    __device__ __forceinline__ void add_partial(int i, const A& x) { Op::merge(a[i], x); }
+    __device__ __forceinline__ void settle() {}
+    __device__ __forceinline__ void flush() {}
+};
+
+// float64 as float pairs, one column (K = 1): scalar state with periodic renormalisation.
+template <> struct VecAcc<AddF64S, 1> {
+    F64Run a[1];
+    __device__ __forceinline__ void zero() { a[0] = AddF64S::zero(); }
+    __device__ __forceinline__ void add(const DF* v) { AddF64S::add(a[0], v[0]); }
+    __device__ __forceinline__ void merge(const VecAcc& o) { AddF64S::merge(a[0], o.a[0]); }
+    __device__ __forceinline__ VecAcc shfl_xor(int m) const { return {{AddF64S::shfl_xor(a[0], m)}}; }
+    __device__ __forceinline__ VecAcc shfl_up(int d) const { return {{AddF64S::shfl_up(a[0], d)}}; }
+    __device__ __forceinline__ F64Run get(int) const { return a[0]; }
+    __device__ __forceinline__ void add_partial(int, const F64Run& x) { AddF64S::merge(a[0], x); }
+    __device__ __forceinline__ void settle() { AddF64S::settle(a[0]); }
+    __device__ __forceinline__ void flush() { AddF64S::flush(a[0]); }
+};
+
+// Compensated float32, columns in pairs.
+template <int NP> struct PackedF32C {
+    float2 hi[NP], lo[NP];
+    __device__ __forceinline__ void zero() {
+#pragma unroll
+        for (int j = 0; j < NP; j++) hi[j] = lo[j] = make_float2(0.0f, 0.0f);
+    }
+    __device__ __forceinline__ void add(const float* v) {
+#pragma unroll
+        for (int j = 0; j < NP; j++) {
+            float2 s, e;
+            two_sum2(hi[j], make_float2(v[2 * j], v[2 * j + 1]), s, e);
+            lo[j] = add2(lo[j], e);
+            hi[j] = s;
+        }
+    }
+    __device__ __forceinline__ void merge(const PackedF32C& o) {
+#pragma unroll
+        for (int j = 0; j < NP; j++) {
+            float2 s, e;
+            two_sum2(hi[j], o.hi[j], s, e);
+            lo[j] = add2(lo[j], add2(o.lo[j], e));
+            hi[j] = s;
+        }
+    }
+    __device__ __forceinline__ PackedF32C shfl_xor(int m) const {
+        PackedF32C r;
+#pragma unroll
+        for (int j = 0; j < NP; j++) {
+            r.hi[j] = shfl_xor2(hi[j], m);
+            r.lo[j] = shfl_xor2(lo[j], m);
+        }
+        return r;
+    }
+    __device__ __forceinline__ PackedF32C shfl_up(int d) const {
+        PackedF32C r;
+#pragma unroll
+        for (int j = 0; j < NP; j++) {
+            r.hi[j] = shfl_up2(hi[j], d);
+            r.lo[j] = shfl_up2(lo[j], d);
+        }
+        return r;
+    }
+    __device__ __forceinline__ F32Pair get(int i) const { return {lane_of(hi[i >> 1], i), lane_of(lo[i >> 1], i)}; }
+    __device__ __forceinline__ void add_partial(int i, const F32Pair& x) {
+        F32Pair r = get(i);
+        AddF32C::merge(r, x);
+        if (i & 1) {
+            hi[i >> 1].y = r.hi;
+            lo[i >> 1].y = r.lo;
+        } else {
+            hi[i >> 1].x = r.hi;
+            lo[i >> 1].x = r.lo;
+        }
+    }
+    __device__ __forceinline__ void settle() {}
+    __device__ __forceinline__ void flush() {}
+};
+template <> struct VecAcc<AddF32C, 2> : PackedF32C<1> {};
+template <> struct VecAcc<AddF32C, 4> : PackedF32C<2> {};
+
+// float64 as float pairs, columns in pairs: double run folds, float2 (hi, lo, plain-sum) state.
+template <int NP> struct PackedF64S {
+    double acc[2 * NP];
+    float2 hi[NP], lo[NP], p[NP];
+    __device__ __forceinline__ void zero() {
+#pragma unroll
+        for (int j = 0; j < NP; j++) {
+            acc[2 * j] = acc[2 * j + 1] = 0.0;
+            hi[j] = lo[j] = p[j] = make_float2(0.0f, 0.0f);
+        }
+    }
+    __device__ __forceinline__ void add(const DF* v) {
+#pragma unroll
+        for (int j = 0; j < NP; j++) {
+            const float2 xh = make_float2(v[2 * j].hi, v[2 * j + 1].hi);
+            const float2 xl = make_float2(v[2 * j].lo, v[2 * j + 1].lo);
+            float2 s, e;
+            two_sum2(hi[j], xh, s, e);
+            lo[j] = add2(lo[j], add2(e, xl));
+            hi[j] = s;
+            p[j] = add2(p[j], xh);
+        }
+    }
+    __device__ __forceinline__ void settle() {
+#pragma unroll
+        for (int j = 0; j < NP; j++) {
+            const float2 h = add2(hi[j], lo[j]);
+            lo[j] = sub2(lo[j], sub2(h, hi[j]));
+            hi[j] = h;
+        }
+    }
+    __device__ __forceinline__ F64Run get(int i) const {
+        return {acc[i], lane_of(hi[i >> 1], i), lane_of(lo[i >> 1], i), lane_of(p[i >> 1], i), 0.0f};
+    }
+    __device__ __forceinline__ void set(int i, const F64Run& r) {
+        acc[i] = r.acc;
+        if (i & 1) {
+            hi[i >> 1].y = r.hi;
+            lo[i >> 1].y = r.lo;
+            p[i >> 1].y = r.p;
+        } else {
+            hi[i >> 1].x = r.hi;
+            lo[i >> 1].x = r.lo;
+            p[i >> 1].x = r.p;
+        }
+    }
+    __device__ __forceinline__ void flush() {
+#pragma unroll
+        for (int i = 0; i < 2 * NP; i++) {
+            F64Run r = get(i);
+            AddF64S::flush(r);
+            set(i, r);
+        }
+    }
+    __device__ __forceinline__ void add_partial(int i, const F64Run& x) {
+        F64Run r = get(i);
+        AddF64S::merge(r, x);
+        set(i, r);
+    }
+    __device__ __forceinline__ void merge(const PackedF64S& o) {
+#pragma unroll
+        for (int i = 0; i < 2 * NP; i++) {
+            F64Run r = get(i);
+            AddF64S::merge(r, o.get(i));
+            set(i, r);
+        }
+    }
+    __device__ __forceinline__ PackedF64S shfl_xor(int m) const {
+        PackedF64S r;
+#pragma unroll
+        for (int j = 0; j < NP; j++) {
+            r.acc[2 * j] = __shfl_xor_sync(FULL_MASK, acc[2 * j], m);
+            r.acc[2 * j + 1] = __shfl_xor_sync(FULL_MASK, acc[2 * j + 1], m);
+            r.hi[j] = shfl_xor2(hi[j], m);
+            r.lo[j] = shfl_xor2(lo[j], m);
+            r.p[j] = shfl_xor2(p[j], m);
+        }
+        return r;
+    }
+    __device__ __forceinline__ PackedF64S shfl_up(int d) const {
+        PackedF64S r;
+#pragma unroll
+        for (int j = 0; j < NP; j++) {
+            r.acc[2 * j] = __shfl_up_sync(FULL_MASK, acc[2 * j], d);
+            r.acc[2 * j + 1] = __shfl_up_sync(FULL_MASK, acc[2 * j + 1], d);
+            r.hi[j] = shfl_up2(hi[j], d);
+            r.lo[j] = shfl_up2(lo[j], d);
+            r.p[j] = shfl_up2(p[j], d);
+        }
+        return r;
+    }
+};
+template <> struct VecAcc<AddF64S, 2> : PackedF64S<1> {};
+
+}  // namespace grgx
