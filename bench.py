@@ -362,6 +362,9 @@ def main():
     compulsory = sum(stats["edges"] * 4 + (stats["nodes"] + 1) * 8 + 2 * stats["nodes"] * K * dt.itemsize
                      for dt, K, d, _ in records)
     launches = sum(t["launches"] for *_, t in records)
+    # the gathers' own ceiling: edge ids + one row per edge, against the measured L2 -> SM bandwidth
+    gathered = sum(stats["edges"] * (4 + K * dt.itemsize) for dt, K, d, _ in records)
+    l2_peak = gx.measure_l2_bandwidth()
     peaks = {}
     pk = ROOT / "MEASURED_PEAKS.json"
     if pk.exists():
@@ -396,7 +399,8 @@ def main():
                    batched_vs_plain(gx, torch, g, stats["edges"], rng2, 48, 8, "K~U{1..8}, UP/DOWN 50/50, float32")]
         g2 = gx.window_tree_grg(max(2, args.samples // 4), max(1, args.mutations * 3 // 10), seed=args.seed + 1)
         g2.upload()
-        serve = served(gx, [g, g2], args.serve_rate, args.serve_seconds, rng2)
+        serve = [served(gx, [g, g2], args.serve_rate, args.serve_seconds, rng2),
+                 served(gx, [g, g2], args.serve_rate * 10, args.serve_seconds / 2.5, rng2)]
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -420,6 +424,10 @@ def main():
                          "dram_frac": None if traffic is None else traffic / (sweep_ms / args.steps / 1e3) / 1e9 / peak,
                          "compulsory_frac": compulsory / (sweep_ms / 1000.0) / 1e9 / peak,
                          "kernel": "grgx::sweep_kernel", "sweep_ms_per_step": sweep_ms / args.steps,
+                         "l2": {"achieved": gathered / (sweep_ms / 1e3) / 1e9, "peak": l2_peak, "unit": "GB/s",
+                                "frac": gathered / (sweep_ms / 1e3) / 1e9 / l2_peak,
+                                "what": "edge ids + one gathered row per edge vs the measured L2->SM read "
+                                        "bandwidth (grgx_measure_l2_bandwidth)"},
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback 6800"},
             "clocks": clk,
             "gpu_launches": launches,

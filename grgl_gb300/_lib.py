@@ -13,6 +13,7 @@ LIB_PATH = Path(__file__).resolve().parent / "libgrgx.so"
 
 OK, ERR_API_MISUSE, ERR_CUDA, ERR_OOM, ERR_BAD_FILE, ERR_UNSUPPORTED, ERR_NO_DEVICE, ERR_TIMEOUT = range(8)
 FLAG_DEVICE_POINTERS, FLAG_F32_PLAIN, FLAG_SYNC, FLAG_OVERWRITE, FLAG_F64_NATIVE = 0x1, 0x2, 0x4, 0x8, 0x10
+FLAG_NO_GRAPH = 0x20
 NOALLOC_SCRATCH_BYTES = 64 << 20  # GRGX_NOALLOC_SCRATCH_BYTES
 
 # Every symbol include/grgx.h declares, with its ctypes signature.
@@ -61,6 +62,7 @@ SIGNATURES = {
     "grgx_server_submit": (_int, [_vp, _u32, ctypes.POINTER(Request), ctypes.POINTER(_u64)]),
     "grgx_server_wait": (_int, [_vp, _u64, ctypes.c_double, ctypes.POINTER(RequestStats)]),
     "grgx_server_destroy": (None, [_vp]),
+    "grgx_measure_l2_bandwidth": (_int, [_u64, _int, ctypes.POINTER(ctypes.c_double)]),
     "grgx_set_timing": (None, [_int]),
     "grgx_last_timing": (_int, [ctypes.POINTER(Timing)]),
 }

@@ -208,8 +208,17 @@ def _torch_dtype_to_np(t):
             torch.int16: np.int16, torch.int8: np.int8, torch.uint8: np.uint8, torch.bool: np.bool_}.get(t)
 
 
+_GRAPHS_ENABLED = [True]
+
+
+def set_graph_replay(enabled: bool):
+    """Enable (default) or disable replaying captured CUDA graphs for small-graph calls."""
+    _GRAPHS_ENABLED[0] = bool(enabled)
+
+
 def _flags(f32_compensated: bool, f64_native: bool) -> int:
-    return ((0 if f32_compensated else _lib.FLAG_F32_PLAIN) | (_lib.FLAG_F64_NATIVE if f64_native else 0))
+    return ((0 if f32_compensated else _lib.FLAG_F32_PLAIN) | (_lib.FLAG_F64_NATIVE if f64_native else 0)
+            | (0 if _GRAPHS_ENABLED[0] else _lib.FLAG_NO_GRAPH))
 
 
 def matmul(grg: GRG, input, direction, emit_all_nodes: bool = False, by_individual: bool = False, init=None,
@@ -336,6 +345,13 @@ def dot_product(grg: GRG, input, direction):
     _check(arr.shape[0] != 0, "dot_product() requires non-empty array input.")
     _check(arr.dtype in _DOT_DTYPES, f"Unsupported numpy dtype: {arr.dtype}")
     return matmul(grg, arr.reshape(1, -1), direction)[0]
+
+
+def measure_l2_bandwidth(nbytes: int = 48 << 20, reps: int = 40) -> float:
+    """Measured L2 -> SM read bandwidth of the current device, GB/s (diagnostic)."""
+    v = ctypes.c_double()
+    _lib.check(_lib.lib().grgx_measure_l2_bandwidth(nbytes, reps, ctypes.byref(v)))
+    return v.value
 
 
 def set_timing(enabled: bool):

@@ -14,6 +14,7 @@ void matmul_impl(grgx_graph* g, int dtype, const void* input, uint64_t in_cols, 
                  void* miss, uint32_t flags, void* stream);
 void set_timing(int enabled);
 grgx_timing last_timing();
+double measure_l2_bandwidth(uint64_t bytes, int reps);
 void matmul_noalloc_impl(grgx_graph* g, int dtype, const void* input, uint64_t in_cols, uint64_t rows, int direction,
                          void* output, uint64_t output_size, void* stream);
 void matmul_batch_impl(grgx_graph* g, const grgx_request* reqs, uint64_t n, uint64_t maxCols, uint32_t flags,
@@ -290,6 +291,13 @@ grgx_status grgx_matmul_noalloc(grgx_graph* g, grgx_dtype dtype, const void* inp
     return guarded([&] {
         GRGX_CHECK(g && input && output, GRGX_ERR_API_MISUSE, "null argument");
         matmul_noalloc_impl(g, dtype, input, input_cols, input_rows, direction, output, output_size, stream);
+    });
+}
+
+grgx_status grgx_measure_l2_bandwidth(uint64_t bytes, int reps, double* gbps) {
+    return guarded([&] {
+        GRGX_CHECK(gbps, GRGX_ERR_API_MISUSE, "null argument");
+        *gbps = measure_l2_bandwidth(bytes, reps);
     });
 }
 

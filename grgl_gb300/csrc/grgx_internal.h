@@ -115,6 +115,13 @@ struct DevicePlanDeleter {
     void operator()(DevicePlan* p) const { destroy_device_plan(p); }
 };
 
+// Captured CUDA graphs of whole calls on small graphs (matmul.cu).
+struct GraphCache;
+void destroy_graph_cache(GraphCache* c);
+struct GraphCacheDeleter {
+    void operator()(GraphCache* c) const { destroy_graph_cache(c); }
+};
+
 // Thread-local error message used by the C ABI.
 void set_last_error(const std::string& msg);
 
@@ -125,6 +132,7 @@ struct grgx_graph {
     std::unique_ptr<grgx::HostGraph> host;
     std::unique_ptr<grgx::HostPlan> plan;
     std::unique_ptr<grgx::DevicePlan, grgx::DevicePlanDeleter> dev;
+    std::unique_ptr<grgx::GraphCache, grgx::GraphCacheDeleter> graphs;  // destroyed before `dev`
     std::mutex mu;  // guards plan/dev creation
     int has_coals = -1;  // cached: every non-sample node has a coalescence count (-1 = not computed)
 };

@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include <cstring>
+#include <map>
 #include <sstream>
 #include <thread>
 
@@ -272,12 +273,12 @@ DevicePlan* ensure_device_plan(grgx_graph* g) {
 uint64_t device_plan_bytes(const grgx_graph* g) { return g->dev ? g->dev->bytes : 0; }
 uint64_t device_plan_levels(const grgx_graph* g) { return g->dev ? g->dev->num_levels : 0; }
 
-void matmul_impl(grgx_graph* g, int dtype, const void* input, uint64_t in_cols, uint64_t rows, int direction,
-                 void* output, uint64_t output_size, int emit_all, int by_indiv, const void* init, int init_kind,
-                 void* miss, uint32_t flags, void* stream_ptr) {
+// Argument checks of validateMatMulInputs (internal_mult.h:130-158) and of the binding, with the
+// reference's messages; host-only, so misuse is reported before any device work.
+void validate_matmul(grgx_graph* g, int dtype, uint64_t in_cols, uint64_t rows, int direction, uint64_t output_size,
+                     int emit_all, int by_indiv, const void* init, int init_kind, void* miss) {
     const HostGraph& hg = *g->host;
     const uint64_t n = hg.num_nodes, N = hg.num_samples, M = hg.num_mutations, P = hg.ploidy;
-    // ---- validation: validateMatMulInputs (internal_mult.h:130-158) and the binding ----------
     GRGX_CHECK(dtype >= GRGX_F64 && dtype <= GRGX_BOOL, GRGX_ERR_API_MISUSE, "Unsupported dtype");
     GRGX_CHECK(direction == GRGX_DIRECTION_DOWN || direction == GRGX_DIRECTION_UP, GRGX_ERR_API_MISUSE,
                "Invalid traversal direction");
@@ -320,6 +321,15 @@ void matmul_impl(grgx_graph* g, int dtype, const void* input, uint64_t in_cols, 
         GRGX_CHECK(g->has_coals == 1, GRGX_ERR_API_MISUSE,
                    "Coalescent counts not available for this GRG (init=XTX won't work)");
     }
+}
+
+void matmul_direct(grgx_graph* g, int dtype, const void* input, uint64_t in_cols, uint64_t rows, int direction,
+                   void* output, uint64_t output_size, int emit_all, int by_indiv, const void* init, int init_kind,
+                   void* miss, uint32_t flags, void* stream_ptr) {
+    const HostGraph& hg = *g->host;
+    const uint64_t n = hg.num_nodes, N = hg.num_samples, M = hg.num_mutations, P = hg.ploidy;
+    validate_matmul(g, dtype, in_cols, rows, direction, output_size, emit_all, by_indiv, init, init_kind, miss);
+    const uint64_t out_cols = output_size / rows;
     DevicePlan* dp = ensure_device_plan(g);
 
     cudaStream_t s = static_cast<cudaStream_t>(stream_ptr);
@@ -531,6 +541,147 @@ void matmul_impl(grgx_graph* g, int dtype, const void* input, uint64_t in_cols, 
         t_last.launches = launches;
     }
     if (!devPtrs || (flags & GRGX_FLAG_SYNC)) GRGX_CUDA(cudaStreamSynchronize(s));
+}
+
+// ---- captured CUDA graphs of whole calls (small graphs) ----------------------------------------
+
+struct GraphEntry {
+    std::mutex mu;
+    cudaStream_t stream = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaEvent_t ready = nullptr, done = nullptr;
+    void *in = nullptr, *out = nullptr, *init = nullptr, *miss = nullptr;
+    size_t inBytes = 0, outBytes = 0, initBytes = 0, missBytes = 0;
+    ~GraphEntry() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (ready) cudaEventDestroy(ready);
+        if (done) cudaEventDestroy(done);
+        for (void* p : {in, out, init, miss})
+            if (p) cudaFree(p);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+struct GraphCache {
+    std::mutex mu;
+    std::map<std::vector<uint64_t>, std::unique_ptr<GraphEntry>> entries;
+};
+
+void destroy_graph_cache(GraphCache* c) { delete c; }
+
+namespace {
+constexpr uint64_t kGraphMaxEdges = 1ull << 25;
+constexpr size_t kGraphMaxEntries = 64;
+}  // namespace
+
+void matmul_impl(grgx_graph* g, int dtype, const void* input, uint64_t in_cols, uint64_t rows, int direction,
+                 void* output, uint64_t output_size, int emit_all, int by_indiv, const void* init, int init_kind,
+                 void* miss, uint32_t flags, void* stream_ptr) {
+    const HostGraph& hg = *g->host;
+    validate_matmul(g, dtype, in_cols, rows, direction, output_size, emit_all, by_indiv, init, init_kind, miss);
+    const bool eligible = !(flags & GRGX_FLAG_NO_GRAPH) && !t_timing && hg.num_edges() <= kGraphMaxEdges &&
+                          hg.num_edges() > 0 && rows > 0 && in_cols > 0 && output_size % rows == 0;
+    if (!eligible) {
+        matmul_direct(g, dtype, input, in_cols, rows, direction, output, output_size, emit_all, by_indiv, init,
+                      init_kind, miss, flags, stream_ptr);
+        return;
+    }
+    const bool devPtrs = (flags & GRGX_FLAG_DEVICE_POINTERS) != 0;
+    const bool overwrite = (flags & GRGX_FLAG_OVERWRITE) != 0;
+    const bool useMiss = miss != nullptr && !hg.miss_node.empty();
+    const size_t esz = io_size(dtype);
+    const uint64_t M = hg.num_mutations, n = hg.num_nodes;
+    cudaStream_t user = static_cast<cudaStream_t>(stream_ptr);
+    const std::vector<uint64_t> key = {static_cast<uint64_t>(dtype), rows, in_cols, output_size,
+                                       static_cast<uint64_t>(direction), static_cast<uint64_t>(emit_all),
+                                       static_cast<uint64_t>(by_indiv), static_cast<uint64_t>(init_kind),
+                                       static_cast<uint64_t>(useMiss),
+                                       static_cast<uint64_t>(flags & (GRGX_FLAG_F32_PLAIN | GRGX_FLAG_F64_NATIVE)),
+                                       static_cast<uint64_t>(overwrite),
+                                       reinterpret_cast<uint64_t>(user), static_cast<uint64_t>(devPtrs)};
+    GraphEntry* e = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g->mu);
+        if (!g->graphs) g->graphs.reset(new GraphCache());
+    }
+    {
+        std::lock_guard<std::mutex> lk(g->graphs->mu);
+        auto it = g->graphs->entries.find(key);
+        if (it != g->graphs->entries.end()) e = it->second.get();
+    }
+    if (e == nullptr) {
+        ensure_device_plan(g);
+        auto ent = std::make_unique<GraphEntry>();
+        ent->inBytes = rows * in_cols * esz;
+        ent->outBytes = output_size * esz;
+        ent->initBytes = (init_kind == GRGX_INIT_VECTOR) ? rows * esz : (init_kind == GRGX_INIT_MATRIX ? rows * n * esz : 0);
+        ent->missBytes = useMiss ? rows * M * esz : 0;
+        GRGX_CUDA(cudaStreamCreateWithFlags(&ent->stream, cudaStreamNonBlocking));
+        GRGX_CUDA(cudaEventCreateWithFlags(&ent->ready, cudaEventDisableTiming));
+        GRGX_CUDA(cudaEventCreateWithFlags(&ent->done, cudaEventDisableTiming));
+        GRGX_CUDA(cudaMalloc(&ent->in, ent->inBytes));
+        GRGX_CUDA(cudaMalloc(&ent->out, ent->outBytes));
+        if (ent->initBytes) GRGX_CUDA(cudaMalloc(&ent->init, ent->initBytes));
+        if (ent->missBytes) GRGX_CUDA(cudaMalloc(&ent->miss, ent->missBytes));
+        // a first direct run on the staging buffers validates the call (errors before capture)
+        GRGX_CUDA(cudaMemsetAsync(ent->in, 0, ent->inBytes, ent->stream));
+        matmul_direct(g, dtype, ent->in, in_cols, rows, direction, ent->out, output_size, emit_all, by_indiv,
+                      init_kind == GRGX_INIT_VECTOR || init_kind == GRGX_INIT_MATRIX ? ent->init : init, init_kind,
+                      useMiss ? ent->miss : nullptr, (flags | GRGX_FLAG_DEVICE_POINTERS | GRGX_FLAG_NO_GRAPH) & ~GRGX_FLAG_SYNC,
+                      ent->stream);
+        GRGX_CUDA(cudaStreamSynchronize(ent->stream));
+        cudaGraph_t graph = nullptr;
+        GRGX_CUDA(cudaStreamBeginCapture(ent->stream, cudaStreamCaptureModeThreadLocal));
+        try {
+            matmul_direct(g, dtype, ent->in, in_cols, rows, direction, ent->out, output_size, emit_all, by_indiv,
+                          init_kind == GRGX_INIT_VECTOR || init_kind == GRGX_INIT_MATRIX ? ent->init : init, init_kind,
+                          useMiss ? ent->miss : nullptr,
+                          (flags | GRGX_FLAG_DEVICE_POINTERS | GRGX_FLAG_NO_GRAPH) & ~GRGX_FLAG_SYNC, ent->stream);
+        } catch (...) {
+            cudaStreamEndCapture(ent->stream, &graph);
+            if (graph) cudaGraphDestroy(graph);
+            throw;
+        }
+        GRGX_CUDA(cudaStreamEndCapture(ent->stream, &graph));
+        const cudaError_t ie = cudaGraphInstantiate(&ent->exec, graph, 0);
+        cudaGraphDestroy(graph);
+        GRGX_CUDA(ie);
+        std::lock_guard<std::mutex> lk(g->graphs->mu);
+        auto it = g->graphs->entries.find(key);
+        if (it != g->graphs->entries.end()) {
+            e = it->second.get();  // another thread won the race
+        } else if (g->graphs->entries.size() < kGraphMaxEntries) {
+            e = ent.get();
+            g->graphs->entries[key] = std::move(ent);
+        } else {
+            // cache full: run directly
+            matmul_direct(g, dtype, input, in_cols, rows, direction, output, output_size, emit_all, by_indiv, init,
+                          init_kind, miss, flags | GRGX_FLAG_NO_GRAPH, stream_ptr);
+            return;
+        }
+    }
+    std::lock_guard<std::mutex> lk(e->mu);
+    const cudaMemcpyKind in = devPtrs ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    const cudaMemcpyKind outk = devPtrs ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    if (devPtrs) {
+        GRGX_CUDA(cudaEventRecord(e->ready, user));
+        GRGX_CUDA(cudaStreamWaitEvent(e->stream, e->ready, 0));
+    }
+    GRGX_CUDA(cudaMemcpyAsync(e->in, input, e->inBytes, in, e->stream));
+    if (e->initBytes) GRGX_CUDA(cudaMemcpyAsync(e->init, init, e->initBytes, in, e->stream));
+    if (e->missBytes) GRGX_CUDA(cudaMemcpyAsync(e->miss, miss, e->missBytes, in, e->stream));
+    if (!overwrite) GRGX_CUDA(cudaMemcpyAsync(e->out, output, e->outBytes, in, e->stream));
+    GRGX_CUDA(cudaGraphLaunch(e->exec, e->stream));
+    GRGX_CUDA(cudaMemcpyAsync(output, e->out, e->outBytes, outk, e->stream));
+    if (e->missBytes && direction == GRGX_DIRECTION_UP)
+        GRGX_CUDA(cudaMemcpyAsync(miss, e->miss, e->missBytes, outk, e->stream));
+    if (devPtrs) {
+        GRGX_CUDA(cudaEventRecord(e->done, e->stream));
+        GRGX_CUDA(cudaStreamWaitEvent(user, e->done, 0));
+        if (flags & GRGX_FLAG_SYNC) GRGX_CUDA(cudaStreamSynchronize(user));
+    } else {
+        GRGX_CUDA(cudaStreamSynchronize(e->stream));
+    }
 }
 
 void set_timing(int enabled) { t_timing = enabled != 0; }

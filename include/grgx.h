@@ -61,6 +61,7 @@ typedef enum { GRGX_INIT_ZERO = 0, GRGX_INIT_VECTOR = 1, GRGX_INIT_MATRIX = 2, G
 #define GRGX_FLAG_SYNC 0x4u            /* wait for the stream before returning */
 #define GRGX_FLAG_OVERWRITE 0x8u       /* write the output instead of adding to it */
 #define GRGX_FLAG_F64_NATIVE 0x10u     /* f64: accumulate on the FP64 pipe instead of as scaled float pairs */
+#define GRGX_FLAG_NO_GRAPH 0x20u       /* never replay a captured CUDA graph for this call */
 
 typedef struct {
     uint64_t num_nodes;
@@ -134,7 +135,12 @@ grgx_status grgx_graph_upload(grgx_graph* g);
  * With GRGX_FLAG_DEVICE_POINTERS the buffers are device pointers and the call is
  * asynchronous on `stream`; otherwise they are host pointers and the call returns when the
  * output (and miss) have been written back.  Validation and messages follow
- * validateMatMulInputs (internal_mult.h:130-158). */
+ * validateMatMulInputs (internal_mult.h:130-158).
+ * On small graphs (at most 2^25 edges) the first call of each shape (dtype, K, direction,
+ * options, stream) captures the whole call into a CUDA graph, which later calls of that shape
+ * replay through staging buffers -- one launch instead of one per level.  The first call of a
+ * shape therefore must not happen inside the caller's own stream capture;
+ * GRGX_FLAG_NO_GRAPH turns this off. */
 grgx_status grgx_matmul(grgx_graph* g, grgx_dtype dtype, const void* input, uint64_t input_cols,
                         uint64_t input_rows, grgx_direction direction, void* output, uint64_t output_size,
                         int emit_all_nodes, int by_individual, const void* init, grgx_init init_kind, void* miss,
@@ -222,6 +228,11 @@ void grgx_server_destroy(grgx_server* s);
 grgx_status grgx_matmul_noalloc(grgx_graph* g, grgx_dtype dtype, const void* input, uint64_t input_cols,
                                 uint64_t input_rows, grgx_direction direction, void* output, uint64_t output_size,
                                 void* stream);
+
+/* Diagnostic, no counterpart in the reference: measured L2 -> SM read bandwidth (GB/s) of the
+ * current device over an L2-resident buffer of `bytes` (>= 1 MiB) read `reps` times -- the
+ * ceiling of the sweep's row gathers when the gathered rows stay in L2. */
+grgx_status grgx_measure_l2_bandwidth(uint64_t bytes, int reps, double* gbps);
 
 /* Device-time breakdown of the last grgx_matmul made by this thread with timing enabled. */
 typedef struct {

@@ -23,7 +23,7 @@ def test_exports_every_declared_symbol(lib_built):
     from grgl_gb300 import _lib
 
     header = (ROOT / "include" / "grgx.h").read_text()
-    declared = set(re.findall(r"\b(grgx_[a-z_]+)\s*\(", header))
+    declared = set(re.findall(r"\b(grgx_[a-z0-9_]+)\s*\(", header))
     assert declared, "no declarations found"
     handle = ctypes.CDLL(str(_lib.LIB_PATH))
     missing = [s for s in sorted(declared) if not hasattr(handle, s)]

@@ -254,3 +254,46 @@ def test_f64_nonfinite_propagates_like_reference(gx, wt):
         with np.errstate(invalid="ignore"):
             scale = oracle.matmul(og, np.where(np.isfinite(V), np.abs(V), 0.0), direction)
         assert np.all(np.abs(got[fin] - ref[fin]) <= 1e-12 * scale[fin] + 1e-300)
+
+
+def test_graph_replay_matches_direct(gx):
+    """Small-graph calls replay a captured CUDA graph: same kernels, so bitwise the same results
+    as the direct path, on repeated calls, several shapes and concurrent threads."""
+    import threading
+    import time
+
+    g = gx.load_immutable_grg(str(GOLDEN / "t200.grg"))
+    rng = np.random.default_rng(8)
+    cases = [(rng.standard_normal((k, g.num_samples)).astype(dt), UP) for k, dt in ((1, np.float64), (5, np.float32))]
+    cases += [(rng.integers(-9, 9, size=(3, g.num_mutations)).astype(np.int32), DOWN)]
+    try:
+        gx.set_graph_replay(False)
+        direct = [gx.matmul(g, V, d) for V, d in cases]
+        t0 = time.perf_counter()
+        for _ in range(20):
+            gx.matmul(g, cases[0][0], UP)
+        t_direct = time.perf_counter() - t0
+    finally:
+        gx.set_graph_replay(True)
+    for _ in range(3):
+        for (V, d), ref in zip(cases, direct):
+            assert np.array_equal(gx.matmul(g, V, d), ref)
+    t0 = time.perf_counter()
+    for _ in range(20):
+        gx.matmul(g, cases[0][0], UP)
+    t_graph = time.perf_counter() - t0
+    print(f"t200 K=1 f64 UP per call: direct {1e3 * t_direct / 20:.3f} ms, graph replay {1e3 * t_graph / 20:.3f} ms")
+    errors = []
+
+    def worker(i):
+        V, d = cases[i % len(cases)]
+        for _ in range(10):
+            if not np.array_equal(gx.matmul(g, V, d), direct[i % len(cases)]):
+                errors.append(i)
+
+    th = [threading.Thread(target=worker, args=(i,)) for i in range(6)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    assert not errors
