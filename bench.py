@@ -50,8 +50,13 @@ def parse_args():
     ap.add_argument("--breakdown", action="store_true",
                     help="print per-matmul device times (3 calls each, CUDA events) instead of the JSON line")
     ap.add_argument("--no-serve", action="store_true", help="skip the batched and served measurements")
-    ap.add_argument("--serve-rate", type=float, default=20.0, help="Poisson arrival rate (requests/s)")
-    ap.add_argument("--serve-seconds", type=float, default=5.0, help="arrival window of the served run")
+    ap.add_argument("--batch-requests", type=int, default=256, help="requests in the batched measurement")
+    ap.add_argument("--serve-rates", default="50,200,1000,2000", help="Poisson arrival rates (requests/s)")
+    ap.add_argument("--serve-seconds", type=float, default=4.0, help="longest arrival window of a served run")
+    ap.add_argument("--serve-requests", type=int, default=96, help="most arrivals in a served run")
+    ap.add_argument("--no-large", action="store_true", help="skip the large-graph measurement")
+    ap.add_argument("--large-samples", type=int, default=1_000_000)
+    ap.add_argument("--large-mutations", type=int, default=300_000)
     return ap.parse_args()
 
 
@@ -164,35 +169,76 @@ def cpu_baseline(args, combos, seconds_budget, threads=None):
                       f"{total_units:.3g} edge*K in {total_t:.1f}s"}
 
 
-def batched_vs_plain(gx, torch, g, E, rng, n_req, kmax, label):
-    """Plain one-request-per-call against matmul_batch on the same requests (device inputs)."""
+def batched_vs_plain(gx, torch, g, E, rng, n_req, kmax, label, std_every=0, err_sample=0):
+    """Plain one-request-per-call against matmul_batch on the same requests (device inputs,
+    float32 compensated).  Every `std_every`-th request is a standardized product (plain path:
+    matmul_standardized).  `err_sample` requests are also computed in float64 and the batched
+    float32 results' error is stated against them, relative to the magnitude of the summed terms."""
     N, M = g.num_samples, g.num_mutations
     reqs = []
-    for _ in range(n_req):
+    for i in range(n_req):
         K = int(rng.integers(1, kmax + 1))
         d = UP if rng.random() < 0.5 else DOWN
-        reqs.append((torch.from_numpy(rng.standard_normal((K, N if d == UP else M)).astype(np.float32)).cuda(), d))
-    units = sum(E * V.shape[0] for V, _ in reqs)
-    for _ in range(2):  # warm both paths (pool, plans)
-        gx.matmul(g, reqs[0][0], reqs[0][1])
+        st = bool(std_every) and i % std_every == 0
+        reqs.append((torch.from_numpy(rng.standard_normal((K, N if d == UP else M)).astype(np.float32)).cuda(), d, st))
+    units = sum(E * V.shape[0] for V, _, _ in reqs)
+
+    def plain(V, d, st):
+        return gx.matmul_standardized(g, V, d) if st else gx.matmul(g, V, d)
+
+    for _ in range(2):  # warm both paths (pool, plans, allele frequencies)
+        plain(*reqs[0])
         gx.matmul_batch(g, reqs[:2])
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for V, d in reqs:
-        gx.matmul(g, V, d)
+    for r in reqs:
+        plain(*r)
     torch.cuda.synchronize()
     t_plain = time.perf_counter() - t0
     t0 = time.perf_counter()
-    gx.matmul_batch(g, reqs)
+    outs = gx.matmul_batch(g, reqs)
     torch.cuda.synchronize()
     t_batch = time.perf_counter() - t0
-    return {"mix": label, "requests": n_req, "plain_edgeK_per_s": units / t_plain,
-            "batched_edgeK_per_s": units / t_batch, "speedup": t_plain / t_batch}
+    res = {"mix": label, "requests": n_req, "standardized_requests": sum(r[2] for r in reqs),
+           "columns": int(sum(V.shape[0] for V, _, _ in reqs)), "plain_edgeK_per_s": units / t_plain,
+           "batched_edgeK_per_s": units / t_batch, "speedup": t_plain / t_batch}
+    if err_sample:
+        worst = {"plain": 0.0, "standardized": 0.0}
+        picks = [i for i in range(n_req) if reqs[i][2]][:err_sample // 2] + \
+                [i for i in range(n_req) if not reqs[i][2]][:err_sample - err_sample // 2]
+        counts = None
+        for i in picks:
+            V, d, st = reqs[i]
+            V64 = V.double()
+            if st:
+                if counts is None:
+                    counts = gx.matmul(g, torch.ones((1, N), dtype=torch.int32, device="cuda"), UP)[0].double()
+                ref = gx.matmul_standardized(g, V64, d)
+                mu = counts / N
+                var = mu * (1 - mu)
+                inv = torch.where(var > 0, 1 / torch.sqrt(torch.where(var > 0, var, torch.ones_like(var))),
+                                  torch.zeros_like(var))
+                if d == UP:
+                    scale = (gx.matmul(g, V64.abs(), UP) + V64.sum(dim=1, keepdim=True).abs() * mu[None, :]) * inv[None, :]
+                else:
+                    W = V64 * inv[None, :]
+                    scale = gx.matmul(g, W.abs(), DOWN) + (W @ mu).abs()[:, None]
+            else:
+                ref = gx.matmul(g, V64, d)
+                scale = gx.matmul(g, V64.abs(), d)
+            e = ((outs[i].double() - ref).abs() / scale.clamp_min(1e-300)).max().item()
+            key = "standardized" if st else "plain"
+            worst[key] = max(worst[key], e)
+        res["f32_max_err_vs_f64"] = {"requests_checked": len(picks), **worst,
+                                     "relative_to": "sum of |terms| per output (|V| X, plus the mean "
+                                                    "correction for standardized)"}
+    return res
 
 
-def served(gx, graphs, rate, seconds, rng):
+def served(gx, graphs, rate, seconds, max_requests, rng):
     """Poisson arrivals over resident graphs (K log-uniform in [1, 256], UP/DOWN and int32/float32
-    mixed), served by the continuous-batching server; against the same requests one per call."""
+    mixed), served by the continuous-batching server; against the same requests one per call.
+    The arrival window is `seconds`, cut short after `max_requests` arrivals."""
     import threading
 
     sizes = [(g.num_samples, g.num_mutations, g.num_edges) for g in graphs]
@@ -203,7 +249,7 @@ def served(gx, graphs, rate, seconds, rng):
             pools[(gi, d, "int32")] = rng.integers(0, 2, size=(256, cols)).astype(np.int32)
             pools[(gi, d, "float32")] = rng.standard_normal((256, cols)).astype(np.float32)
     arrivals, t = [], 0.0
-    while True:
+    while len(arrivals) < max_requests:
         t += rng.exponential(1.0 / rate)
         if t > seconds:
             break
@@ -212,6 +258,8 @@ def served(gx, graphs, rate, seconds, rng):
         d = UP if rng.random() < 0.5 else DOWN
         dt = "int32" if rng.random() < 0.5 else "float32"
         arrivals.append((t, gi, d, pools[(gi, d, dt)][:K]))
+    if not arrivals:
+        return {"arrival_rate_per_s": rate, "requests": 0}
     units = sum(sizes[gi][2] * V.shape[0] for _, gi, _, V in arrivals)
     lat = []
     with gx.Server(workers=3) as srv:
@@ -244,12 +292,69 @@ def served(gx, graphs, rate, seconds, rng):
         gx.matmul(graphs[gi], V, d)
     t_plain = time.perf_counter() - t0
     lat_ms = np.array(lat) * 1e3
-    return {"arrival_rate_per_s": rate, "requests": len(arrivals), "graphs": [
-                {"samples": N, "mutations": M, "edges": E} for N, M, E in sizes],
+    return {"arrival_rate_per_s": rate, "requests": len(arrivals),
+            "arrival_window_s": arrivals[-1][0] if arrivals else 0.0,
             "p50_ms": float(np.percentile(lat_ms, 50)), "p99_ms": float(np.percentile(lat_ms, 99)),
             "served_edgeK_per_s": units / t_served, "plain_sequential_edgeK_per_s": units / t_plain,
-            "mean_batch_requests": float(np.mean(batches)),
-            "note": "served throughput is bounded by the offered load; plain = the same requests one per call"}
+            "mean_batch_requests": float(np.mean(batches))}
+
+
+def large_graph(gx, torch, args, peak):
+    """The large window-tree graph (N=1,000,000 haplotypes, a variant prefix sized to 2-4e9 edges):
+    float32 compensated and float64 at K in {16, 64, 256}, both directions, device inputs.  Each
+    entry: sweep device time (CUDA events), edge*K/s, algorithmic GB/s against the HBM peak, and the
+    float32 result's max error against the float64 result, relative to the sum of |terms| per
+    output (|V| X); the float64 result is checked against native FP64 accumulation at K=16."""
+    t0 = time.perf_counter()
+    g = gx.window_tree_grg(args.large_samples, args.large_mutations, seed=args.seed)
+    t_gen = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    g.upload()
+    torch.cuda.synchronize()
+    t_up = time.perf_counter() - t0
+    stats = graph_stats(g)
+    stats["device_bytes"] = g.info()["device_bytes"]
+    E = stats["edges"]
+    rng = np.random.default_rng(5)
+    rows = []
+    gx.set_timing(True)
+    for K in (16, 64, 256):
+        for d in (UP, DOWN):
+            cols = stats["samples"] if d == UP else stats["mutations"]
+            V32 = torch.from_numpy(rng.standard_normal((K, cols)).astype(np.float32)).cuda()
+            V64 = V32.double()
+            for V in (V64, V32):
+                res = None
+                for _ in range(2):  # the second call is the timed one
+                    res = gx.matmul(g, V, d)
+                t = gx.last_timing()
+                s = V.element_size()
+                rows.append({"dtype": "float64" if s == 8 else "float32", "K": K, "dir": "UP" if d == UP else "DOWN",
+                             "sweep_ms": t["sweep_ms"], "total_ms": t["total_ms"],
+                             "edgeK_per_s": E * K / (t["sweep_ms"] / 1e3),
+                             "alg_GBps": alg_bytes(stats, K, s, d) / (t["sweep_ms"] / 1e3) / 1e9,
+                             "hbm_frac": alg_bytes(stats, K, s, d) / (t["sweep_ms"] / 1e3) / 1e9 / peak})
+                if s == 8:
+                    y64 = res
+                else:
+                    y32 = res
+            scale = gx.matmul(g, V32.abs(), d, f32_compensated=False).double().clamp_min(1e-30)
+            rows[-1]["max_err_vs_f64"] = ((y32.double() - y64).abs() / scale).max().item()
+            if K == 16:
+                y64n = gx.matmul(g, V64, d, f64_native=True)
+                rows[-2]["max_err_vs_native_f64"] = ((y64 - y64n).abs() / scale).max().item()
+            del y32, y64, res, V32, V64
+    gx.set_timing(False)
+    units = sum(E * r["K"] for r in rows)
+    secs = sum(r["sweep_ms"] for r in rows) / 1e3
+    abytes = sum(alg_bytes(stats, r["K"], 8 if r["dtype"] == "float64" else 4, UP if r["dir"] == "UP" else DOWN)
+                 for r in rows)
+    del g
+    torch.cuda.empty_cache()
+    return {"graph": dict(stats, note=f"variant prefix M'={args.large_mutations} of the 10,000,000-variant "
+                                      "generator run, sized to the 2-4e9-edge budget"),
+            "edgeK_per_s": units / secs, "alg_GBps": abytes / secs / 1e9, "hbm_frac": abytes / secs / 1e9 / peak,
+            "matmuls": rows, "setup_s": {"generate": t_gen, "plan_upload": t_up}}
 
 
 def run_reference(args):
@@ -392,15 +497,26 @@ def main():
         e2e_s = time.perf_counter() - t0
         e2e_value = units_per_step * e2e_steps * world / e2e_s
 
-    batched = serve = None
+    batched = serve = large = None
     if rank == 0 and not args.no_serve:
         rng2 = np.random.default_rng(11)
-        batched = [batched_vs_plain(gx, torch, g, stats["edges"], rng2, 48, 128, "K~U{1..128}, UP/DOWN 50/50, float32"),
-                   batched_vs_plain(gx, torch, g, stats["edges"], rng2, 48, 8, "K~U{1..8}, UP/DOWN 50/50, float32")]
+        nb = args.batch_requests
+        batched = [batched_vs_plain(gx, torch, g, stats["edges"], rng2, nb, 128,
+                                    "K~U{1..128}, UP/DOWN 50/50, float32 compensated, half N(0,1) and half "
+                                    "standardized inputs", std_every=2, err_sample=8),
+                   batched_vs_plain(gx, torch, g, stats["edges"], rng2, nb, 8,
+                                    "K~U{1..8}, UP/DOWN 50/50, float32 compensated, N(0,1) inputs")]
         g2 = gx.window_tree_grg(max(2, args.samples // 4), max(1, args.mutations * 3 // 10), seed=args.seed + 1)
         g2.upload()
-        serve = [served(gx, [g, g2], args.serve_rate, args.serve_seconds, rng2),
-                 served(gx, [g, g2], args.serve_rate * 10, args.serve_seconds / 2.5, rng2)]
+        serve = {"graphs": [graph_stats(x) for x in (g, g2)],
+                 "mix": "K log-uniform in [1, 256], UP/DOWN 50/50, int32 0/1 and float32 N(0,1) 50/50, "
+                        "70% of requests on the first graph",
+                 "plain": "the same requests one per call, sequentially",
+                 "runs": [served(gx, [g, g2], float(r), args.serve_seconds, args.serve_requests, rng2)
+                          for r in args.serve_rates.split(",")]}
+        del g2
+    if rank == 0 and not args.no_large:
+        large = large_graph(gx, torch, args, peak)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -435,6 +551,7 @@ def main():
             "cpu_baseline": cpu,
             "batched_vs_plain": batched,
             "served": serve,
+            "large_graph": large,
             "setup_s": {"generate": t_gen, "plan_upload": t_up},
         }
         print(json.dumps(line), flush=True)

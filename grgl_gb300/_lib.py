@@ -14,6 +14,7 @@ LIB_PATH = Path(__file__).resolve().parent / "libgrgx.so"
 OK, ERR_API_MISUSE, ERR_CUDA, ERR_OOM, ERR_BAD_FILE, ERR_UNSUPPORTED, ERR_NO_DEVICE, ERR_TIMEOUT = range(8)
 FLAG_DEVICE_POINTERS, FLAG_F32_PLAIN, FLAG_SYNC, FLAG_OVERWRITE, FLAG_F64_NATIVE = 0x1, 0x2, 0x4, 0x8, 0x10
 FLAG_NO_GRAPH = 0x20
+REQUEST_STANDARDIZED = 0x1
 NOALLOC_SCRATCH_BYTES = 64 << 20  # GRGX_NOALLOC_SCRATCH_BYTES
 
 # Every symbol include/grgx.h declares, with its ctypes signature.
@@ -33,7 +34,7 @@ class Timing(ctypes.Structure):
 
 class Request(ctypes.Structure):
     _fields_ = [("dtype", ctypes.c_int), ("direction", ctypes.c_int), ("rows", _u64), ("input", _vp),
-                ("output", _vp)]
+                ("output", _vp), ("options", _u32)]
 
 
 class RequestStats(ctypes.Structure):

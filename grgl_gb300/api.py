@@ -400,9 +400,10 @@ def matmul_standardized(grg: GRG, input, direction, *, f32_compensated: bool = T
 # ---- batching and serving ----------------------------------------------------------------------
 
 
-def _request_for(grg, x, direction):
-    """Validate one plain request and allocate its output (host or device like the input)."""
+def _request_for(grg, x, direction, standardized=False):
+    """Validate one request and allocate its output (host or device like the input)."""
     direction = TraversalDirection(int(direction))
+    opts = _lib.REQUEST_STANDARDIZED if standardized else 0
     cols = grg.num_samples if direction == UP else grg.num_mutations
     out_cols = grg.num_mutations if direction == UP else grg.num_samples
     if _is_torch_cuda(x):
@@ -416,7 +417,9 @@ def _request_for(grg, x, direction):
                else "Input vector is not size M (numMutations)")
         out = torch.empty((x.shape[0], out_cols), dtype=x.dtype, device=x.device)
         code = _DTYPE_CODES[np.dtype(npd)]
-        return x, out, _lib.Request(code, int(direction), x.shape[0], x.data_ptr(), out.data_ptr())
+        if standardized:
+            _check(npd in (np.float32, np.float64), "standardized products take float32 or float64 input")
+        return x, out, _lib.Request(code, int(direction), x.shape[0], x.data_ptr(), out.data_ptr(), opts)
     _check(isinstance(x, np.ndarray), f"Unsupported numpy dtype: {np.asarray(x).dtype}")
     x = np.ascontiguousarray(x)
     _check(x.ndim == 2, "matmul() only support two dimensional numpy arrays as input.")
@@ -425,18 +428,23 @@ def _request_for(grg, x, direction):
     _check(x.shape[1] == cols,
            "Input vector is not size N (numSamples, or numIndividuals depending on flags)" if direction == UP
            else "Input vector is not size M (numMutations)")
+    if standardized:
+        _check(x.dtype in (np.float32, np.float64), "standardized products take float32 or float64 input")
     out = np.empty((x.shape[0], out_cols), dtype=x.dtype)
-    return x, out, _lib.Request(_DTYPE_CODES[x.dtype], int(direction), x.shape[0], x.ctypes.data, out.ctypes.data)
+    return x, out, _lib.Request(_DTYPE_CODES[x.dtype], int(direction), x.shape[0], x.ctypes.data, out.ctypes.data,
+                                opts)
 
 
 def matmul_batch(grg: GRG, requests, max_cols: int = 0, *, f32_compensated: bool = True, f64_native: bool = False):
-    """Several plain products on one graph, coalesced into shared traversals.
+    """Several products on one graph, coalesced into shared traversals.
 
-    ``requests`` is a list of ``(input, direction)``; inputs are all numpy arrays or all CUDA
-    tensors.  Returns the outputs in order.  Requests of the same direction and dtype are
-    stacked into traversals of at most ``max_cols`` rows (0 = the sweep's natural width).
+    ``requests`` is a list of ``(input, direction)`` or ``(input, direction, standardized)``;
+    inputs are all numpy arrays or all CUDA tensors.  A standardized request computes what
+    ``matmul_standardized`` does.  Returns the outputs in order.  Requests of the same direction
+    and dtype are stacked into traversals of at most ``max_cols`` rows (0 = the sweep's natural
+    width).
     """
-    prepared = [_request_for(grg, x, d) for x, d in requests]
+    prepared = [_request_for(grg, r[0], r[1], bool(r[2]) if len(r) > 2 else False) for r in requests]
     if not prepared:
         return []
     dev = _is_torch_cuda(prepared[0][0])
@@ -474,8 +482,8 @@ class Server:
         self._graphs.append(grg)
         return int(gid.value)
 
-    def submit(self, graph_id: int, input, direction) -> int:
-        x, out, req = _request_for(self._graphs[graph_id], input, direction)
+    def submit(self, graph_id: int, input, direction, standardized: bool = False) -> int:
+        x, out, req = _request_for(self._graphs[graph_id], input, direction, standardized)
         _check(not _is_torch_cuda(x), "the server takes host (numpy) arrays")
         t = ctypes.c_uint64()
         _lib.check(_lib.lib().grgx_server_submit(self._h, graph_id, ctypes.byref(req), ctypes.byref(t)))

@@ -20,6 +20,15 @@ void matmul_impl(grgx_graph* g, int dtype, const void* input, uint64_t in_cols, 
                  void* output, uint64_t output_size, int emit_all, int by_indiv, const void* init, int init_kind,
                  void* miss, uint32_t flags, void* stream);
 
+void matmul_standardized_impl(grgx_graph* g, int dtype, const void* input, uint64_t in_cols, uint64_t rows,
+                              int direction, void* output, uint64_t output_size, uint32_t flags, void* stream);
+DevicePlan* standardized_plan(grgx_graph* g, cudaStream_t s);
+void standardized_prepare_down(int dtype, const DevicePlan* dp, void* V, long long K, long long M, double* c,
+                               cudaStream_t s);
+void standardized_finish_down(int dtype, void* Y, const double* c, long long K, long long N, cudaStream_t s);
+void standardized_finish_up(int dtype, const DevicePlan* dp, const void* V, long long K, long long N, void* VX,
+                            long long M, double* red, cudaStream_t s);
+
 namespace {
 
 #define BATCH_CUDA(call)                                                                             \
@@ -59,6 +68,9 @@ void matmul_batch_impl(grgx_graph* g, const grgx_request* reqs, uint64_t n, uint
         GRGX_CHECK(r.direction == GRGX_DIRECTION_DOWN || r.direction == GRGX_DIRECTION_UP, GRGX_ERR_API_MISUSE,
                    "Invalid traversal direction");
         GRGX_CHECK(r.dtype >= GRGX_F64 && r.dtype <= GRGX_BOOL, GRGX_ERR_API_MISUSE, "Unsupported dtype");
+        GRGX_CHECK((r.options & ~GRGX_REQUEST_STANDARDIZED) == 0, GRGX_ERR_API_MISUSE, "Unknown request options");
+        GRGX_CHECK(!(r.options & GRGX_REQUEST_STANDARDIZED) || r.dtype == GRGX_F32 || r.dtype == GRGX_F64,
+                   GRGX_ERR_UNSUPPORTED, "standardized products take float32 or float64 input");
         groups[{static_cast<int>(r.direction), static_cast<int>(r.dtype)}].push_back(i);
     }
     const uint32_t passFlags = (flags & (GRGX_FLAG_F32_PLAIN | GRGX_FLAG_F64_NATIVE)) | GRGX_FLAG_DEVICE_POINTERS |
@@ -79,11 +91,21 @@ void matmul_batch_impl(grgx_graph* g, const grgx_request* reqs, uint64_t n, uint
             while (j < idx.size() && rowsTotal + reqs[idx[j]].rows <= width) rowsTotal += reqs[idx[j++]].rows;
             if (j == i + 1) {
                 const grgx_request& r = reqs[idx[i]];
-                matmul_impl(g, dtype, r.input, cols, r.rows, direction, r.output, r.rows * outCols, 0, 0, nullptr,
-                            GRGX_INIT_ZERO, nullptr, (flags & ~GRGX_FLAG_SYNC) | GRGX_FLAG_OVERWRITE, stream);
+                if (r.options & GRGX_REQUEST_STANDARDIZED)
+                    matmul_standardized_impl(g, dtype, r.input, cols, r.rows, direction, r.output, r.rows * outCols,
+                                             flags & ~GRGX_FLAG_SYNC, stream);
+                else
+                    matmul_impl(g, dtype, r.input, cols, r.rows, direction, r.output, r.rows * outCols, 0, 0,
+                                nullptr, GRGX_INIT_ZERO, nullptr, (flags & ~GRGX_FLAG_SYNC) | GRGX_FLAG_OVERWRITE,
+                                stream);
                 i = j;
                 continue;
             }
+            bool anyStd = false;
+            for (size_t k = i; k < j; k++) anyStd |= (reqs[idx[k]].options & GRGX_REQUEST_STANDARDIZED) != 0;
+            DevicePlan* dp = anyStd ? standardized_plan(g, s) : nullptr;
+            double* red = nullptr;
+            if (anyStd) BATCH_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&red), rowsTotal * sizeof(double), s));
             void* in = nullptr;
             void* out = nullptr;
             BATCH_CUDA(cudaMallocAsync(&in, rowsTotal * cols * es, s));
@@ -91,8 +113,12 @@ void matmul_batch_impl(grgx_graph* g, const grgx_request* reqs, uint64_t n, uint
             uint64_t row = 0;
             for (size_t k = i; k < j; k++) {
                 const grgx_request& r = reqs[idx[k]];
-                BATCH_CUDA(cudaMemcpyAsync(static_cast<char*>(in) + row * cols * es, r.input, r.rows * cols * es,
+                char* rowsIn = static_cast<char*>(in) + row * cols * es;
+                BATCH_CUDA(cudaMemcpyAsync(rowsIn, r.input, r.rows * cols * es,
                                            dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+                if ((r.options & GRGX_REQUEST_STANDARDIZED) && direction == GRGX_DIRECTION_DOWN)
+                    standardized_prepare_down(dtype, dp, rowsIn, static_cast<long long>(r.rows),
+                                              static_cast<long long>(cols), red + row, s);
                 row += r.rows;
             }
             matmul_impl(g, dtype, in, cols, rowsTotal, direction, out, rowsTotal * outCols, 0, 0, nullptr,
@@ -100,13 +126,24 @@ void matmul_batch_impl(grgx_graph* g, const grgx_request* reqs, uint64_t n, uint
             row = 0;
             for (size_t k = i; k < j; k++) {
                 const grgx_request& r = reqs[idx[k]];
-                BATCH_CUDA(cudaMemcpyAsync(r.output, static_cast<char*>(out) + row * outCols * es,
+                char* rowsOut = static_cast<char*>(out) + row * outCols * es;
+                if (r.options & GRGX_REQUEST_STANDARDIZED) {
+                    if (direction == GRGX_DIRECTION_DOWN)
+                        standardized_finish_down(dtype, rowsOut, red + row, static_cast<long long>(r.rows),
+                                                 static_cast<long long>(outCols), s);
+                    else
+                        standardized_finish_up(dtype, dp, static_cast<char*>(in) + row * cols * es,
+                                               static_cast<long long>(r.rows), static_cast<long long>(cols), rowsOut,
+                                               static_cast<long long>(outCols), red + row, s);
+                }
+                BATCH_CUDA(cudaMemcpyAsync(r.output, rowsOut,
                                            r.rows * outCols * es,
                                            dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
                 row += r.rows;
             }
             BATCH_CUDA(cudaFreeAsync(in, s));
             BATCH_CUDA(cudaFreeAsync(out, s));
+            if (red) BATCH_CUDA(cudaFreeAsync(red, s));
             i = j;
         }
     }

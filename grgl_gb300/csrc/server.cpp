@@ -244,6 +244,11 @@ grgx_status grgx_server_submit(grgx_server* s, uint32_t graph_id, const grgx_req
                    GRGX_ERR_API_MISUSE, "Invalid traversal direction");
         GRGX_CHECK(request->dtype >= GRGX_F64 && request->dtype <= GRGX_BOOL, GRGX_ERR_API_MISUSE,
                    "Unsupported dtype");
+        GRGX_CHECK((request->options & ~GRGX_REQUEST_STANDARDIZED) == 0, GRGX_ERR_API_MISUSE,
+                   "Unknown request options");
+        GRGX_CHECK(!(request->options & GRGX_REQUEST_STANDARDIZED) || request->dtype == GRGX_F32 ||
+                       request->dtype == GRGX_F64,
+                   GRGX_ERR_UNSUPPORTED, "standardized products take float32 or float64 input");
         auto q = std::make_shared<grgx_server::Req>();
         q->r = *request;
         {

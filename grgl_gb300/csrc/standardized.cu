@@ -62,9 +62,10 @@ __global__ void row_sum_kernel(const T* __restrict__ V, long long K, long long c
     }
 }
 
+// W may alias V (the batched path scales stacked rows in place).
 template <typename T>
-__global__ void down_prepare_kernel(const T* __restrict__ V, long long K, long long M, const double* __restrict__ freq,
-                                    const double* __restrict__ invSigma, T* __restrict__ W, double* __restrict__ c) {
+__global__ void down_prepare_kernel(const T* V, long long K, long long M, const double* __restrict__ freq,
+                                    const double* __restrict__ invSigma, T* W, double* __restrict__ c) {
     for (long long k = blockIdx.x; k < K; k += gridDim.x) {
         double acc = 0.0;
         for (long long j = threadIdx.x; j < M; j += blockDim.x) {
@@ -77,10 +78,10 @@ __global__ void down_prepare_kernel(const T* __restrict__ V, long long K, long l
     }
 }
 
+// out may alias VX.
 template <typename T>
-__global__ void up_finish_kernel(const T* __restrict__ VX, const double* __restrict__ rowSum,
-                                 const double* __restrict__ freq, const double* __restrict__ invSigma, long long K,
-                                 long long M, T* __restrict__ out) {
+__global__ void up_finish_kernel(const T* VX, const double* __restrict__ rowSum, const double* __restrict__ freq,
+                                 const double* __restrict__ invSigma, long long K, long long M, T* out) {
     const long long total = K * M;
     for (long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x; x < total; x += (long long)gridDim.x * blockDim.x) {
         const long long k = x / M, j = x % M;
@@ -156,6 +157,52 @@ void run(grgx_graph* g, DevicePlan* dp, int dtype, const T* in, long long K, int
 }
 
 }  // namespace
+
+// ---- pieces for stacked traversals (grgx_matmul_batch, the server) ----------------------------
+
+DevicePlan* standardized_plan(grgx_graph* g, cudaStream_t s) {
+    DevicePlan* dp = ensure_device_plan(g);
+    ensure_stats(g, dp, s);
+    return dp;
+}
+
+// V (K x M, in place) becomes W = V diag(1/sigma); c[k] = mu^T w_k.
+void standardized_prepare_down(int dtype, const DevicePlan* dp, void* V, long long K, long long M, double* c,
+                               cudaStream_t s) {
+    const unsigned rowBlocks = static_cast<unsigned>(std::min<long long>(K, 65535));
+    if (dtype == GRGX_F64)
+        down_prepare_kernel<double><<<rowBlocks, 256, 0, s>>>(static_cast<double*>(V), K, M, dp->freq, dp->inv_sigma,
+                                                              static_cast<double*>(V), c);
+    else
+        down_prepare_kernel<float><<<rowBlocks, 256, 0, s>>>(static_cast<float*>(V), K, M, dp->freq, dp->inv_sigma,
+                                                             static_cast<float*>(V), c);
+    GRGX_CUDA(cudaGetLastError());
+}
+
+// Y (K x N, in place) -= c[k].
+void standardized_finish_down(int dtype, void* Y, const double* c, long long K, long long N, cudaStream_t s) {
+    if (dtype == GRGX_F64)
+        down_finish_kernel<double><<<grid_for(K * N), 256, 0, s>>>(static_cast<double*>(Y), c, K, N);
+    else
+        down_finish_kernel<float><<<grid_for(K * N), 256, 0, s>>>(static_cast<float*>(Y), c, K, N);
+    GRGX_CUDA(cudaGetLastError());
+}
+
+// VX (K x M, in place) becomes (VX - (V 1) mu^T) diag(1/sigma); `red` holds K doubles.
+void standardized_finish_up(int dtype, const DevicePlan* dp, const void* V, long long K, long long N, void* VX,
+                            long long M, double* red, cudaStream_t s) {
+    const unsigned rowBlocks = static_cast<unsigned>(std::min<long long>(K, 65535));
+    if (dtype == GRGX_F64) {
+        row_sum_kernel<double><<<rowBlocks, 256, 0, s>>>(static_cast<const double*>(V), K, N, red);
+        up_finish_kernel<double><<<grid_for(K * M), 256, 0, s>>>(static_cast<double*>(VX), red, dp->freq,
+                                                                 dp->inv_sigma, K, M, static_cast<double*>(VX));
+    } else {
+        row_sum_kernel<float><<<rowBlocks, 256, 0, s>>>(static_cast<const float*>(V), K, N, red);
+        up_finish_kernel<float><<<grid_for(K * M), 256, 0, s>>>(static_cast<float*>(VX), red, dp->freq,
+                                                                dp->inv_sigma, K, M, static_cast<float*>(VX));
+    }
+    GRGX_CUDA(cudaGetLastError());
+}
 
 void matmul_standardized_impl(grgx_graph* g, int dtype, const void* input, uint64_t in_cols, uint64_t rows,
                               int direction, void* output, uint64_t output_size, uint32_t flags, void* stream) {

@@ -162,13 +162,18 @@ grgx_status grgx_matmul_standardized(grgx_graph* g, grgx_dtype dtype, const void
 
 /* One request of a batch or of the server: the plain product (no init, miss, emit_all_nodes or
  * by_individual) of `rows` x cols `input` in `direction`, written to `output` (rows x out_cols,
- * overwritten).  Host or device memory as the call's flags say. */
+ * overwritten).  Host or device memory as the call's flags say.  With
+ * GRGX_REQUEST_STANDARDIZED in `options` the product is the one grgx_matmul_standardized
+ * computes (float32/float64 only); it still shares the traversal with the plain requests
+ * stacked beside it. */
+#define GRGX_REQUEST_STANDARDIZED 0x1u
 typedef struct {
     grgx_dtype dtype;
     grgx_direction direction;
     uint64_t rows;
     const void* input;
     void* output;
+    uint32_t options;
 } grgx_request;
 
 /* No counterpart in the reference (its callers loop over matMul calls).  Runs `n` requests on

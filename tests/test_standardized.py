@@ -56,3 +56,41 @@ def test_standardized_rejects_integer_input(env):
     gx, g, _ = env
     with pytest.raises(RuntimeError, match="float32 or float64"):
         gx.matmul_standardized(g, np.ones((1, g.num_samples), dtype=np.int32), UP)
+
+
+def test_standardized_requests_batched_and_served(env):
+    """Standardized requests stacked beside plain ones (one traversal) and through the server
+    give the standardized product; the plain requests beside them are unaffected."""
+    import torch
+
+    gx, g, og = env
+    rng = np.random.default_rng(4)
+    reqs = []
+    for i in range(12):
+        d = UP if i % 2 else DOWN
+        dt = np.float32 if i % 3 else np.float64
+        V = rng.standard_normal((int(rng.integers(1, 9)), g.num_samples if d == UP else g.num_mutations)).astype(dt)
+        reqs.append((V, d, i % 4 != 0))
+    for outs in (gx.matmul_batch(g, reqs),
+                 [o.cpu().numpy() for o in gx.matmul_batch(g, [(torch.from_numpy(V).cuda(), d, st)
+                                                               for V, d, st in reqs])]):
+        for (V, d, st), got in zip(reqs, outs):
+            rtol = 1e-6 if V.dtype == np.float32 else 1e-12
+            if st:
+                ref, scale = oracle.standardized(og, V, d, return_scale=True)
+            else:
+                ref = oracle.matmul(og, V.astype(np.float64), d)
+                scale = oracle.matmul(og, np.abs(V).astype(np.float64), d)
+            err = np.abs(got.astype(np.float64) - ref)
+            assert np.all(err <= rtol * scale + 1e-300), (d, st, V.dtype)
+    with gx.Server(workers=2) as srv:
+        gid = srv.add_graph(g)
+        tickets = [srv.submit(gid, V, d, standardized=st) for V, d, st in reqs]
+        for (V, d, st), t in zip(reqs, tickets):
+            got, _ = srv.result(t, timeout=120)
+            if st:
+                ref, scale = oracle.standardized(og, V, d, return_scale=True)
+                rtol = 1e-6 if V.dtype == np.float32 else 1e-12
+                assert np.all(np.abs(got.astype(np.float64) - ref) <= rtol * scale + 1e-300)
+    with pytest.raises(RuntimeError, match="float32 or float64"):
+        gx.matmul_batch(g, [(np.ones((1, g.num_samples), dtype=np.int32), UP, True)])
