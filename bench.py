@@ -55,6 +55,7 @@ def parse_args():
     ap.add_argument("--serve-seconds", type=float, default=4.0, help="longest arrival window of a served run")
     ap.add_argument("--serve-requests", type=int, default=96, help="most arrivals in a served run")
     ap.add_argument("--no-large", action="store_true", help="skip the large-graph measurement")
+    ap.add_argument("--no-autotune", action="store_true", help="run the default launch shapes (no tuning pass)")
     ap.add_argument("--large-samples", type=int, default=1_000_000)
     ap.add_argument("--large-mutations", type=int, default=300_000)
     return ap.parse_args()
@@ -437,6 +438,18 @@ def main():
             print(json.dumps(rec), flush=True)
         return
 
+    # launch-shape autotuning: each level of every (dtype, K, direction) of the step
+    tune = None
+    if not args.no_autotune:
+        gx.autotune_clear()
+        t0 = time.perf_counter()
+        levels_tuned = 0
+        for dt, K, d in dict.fromkeys(combos):
+            levels_tuned += gx.autotune(g, dt, K, d).count("level ")
+        torch.cuda.synchronize()
+        tune = {"seconds": time.perf_counter() - t0, "levels_tuned": levels_tuned,
+                "table_entries": len(gx.autotune_table().strip().splitlines())}
+
     # warm-up
     for _ in range(args.warmup):
         step(dev_inputs, None)
@@ -460,6 +473,19 @@ def main():
     ms = float(ms_t.item())
     units_per_step = sum(stats["edges"] * K for _, K, _ in combos)
     value = units_per_step * args.steps * world / (ms / 1000.0)
+
+    if tune is not None:
+        # the same step on the default shapes, for the tuner's gain (untimed for `value`)
+        saved = gx.autotune_table()
+        gx.autotune_clear()
+        gx.set_timing(True)
+        step(dev_inputs, None)
+        recs = []
+        step(dev_inputs, recs)
+        gx.set_timing(False)
+        gx.autotune_load(saved)
+        tune["sweep_ms_per_step_default_shapes"] = sum(t["sweep_ms"] for *_, t in recs)
+        tune["sweep_ms_per_step_tuned"] = sum(t["sweep_ms"] for *_, t in records) / args.steps
 
     # roofline of the sweep kernel over the timed region
     sweep_ms = sum(t["sweep_ms"] for *_, t in records)
@@ -552,6 +578,7 @@ def main():
             "batched_vs_plain": batched,
             "served": serve,
             "large_graph": large,
+            "autotune": tune,
             "setup_s": {"generate": t_gen, "plan_upload": t_up},
         }
         print(json.dumps(line), flush=True)

@@ -64,6 +64,10 @@ SIGNATURES = {
     "grgx_server_wait": (_int, [_vp, _u64, ctypes.c_double, ctypes.POINTER(RequestStats)]),
     "grgx_server_destroy": (None, [_vp]),
     "grgx_measure_l2_bandwidth": (_int, [_u64, _int, ctypes.POINTER(ctypes.c_double)]),
+    "grgx_autotune": (_int, [c_graph_p, _int, _u64, _int, _u32, ctypes.c_char_p, _u64, ctypes.POINTER(_u64)]),
+    "grgx_autotune_export": (_int, [ctypes.c_char_p, _u64, ctypes.POINTER(_u64)]),
+    "grgx_autotune_import": (_int, [ctypes.c_char_p]),
+    "grgx_autotune_clear": (None, []),
     "grgx_set_timing": (None, [_int]),
     "grgx_last_timing": (_int, [ctypes.POINTER(Timing)]),
 }

@@ -435,6 +435,39 @@ def _request_for(grg, x, direction, standardized=False):
                                 opts)
 
 
+def autotune(grg: GRG, dtype, rows: int, direction, *, f32_compensated: bool = True,
+             f64_native: bool = False) -> str:
+    """Measure every launch shape on each level of one traversal of ``grg`` for ``rows`` x cols
+    inputs of ``dtype`` in ``direction`` and record the winners in the process-wide shape table
+    (keyed on the level's width, mean degree, the storage kind and K).  Returns the per-level
+    report.  Later calls on any graph whose levels match an entry run the tuned shape."""
+    code = _DTYPE_CODES[np.dtype(dtype)]
+    need = ctypes.c_uint64()
+    buf = ctypes.create_string_buffer(1 << 16)
+    _lib.check(_lib.lib().grgx_autotune(grg._h, code, int(rows), int(TraversalDirection(int(direction))),
+                                        _flags(f32_compensated, f64_native), buf, len(buf), ctypes.byref(need)))
+    return buf.value.decode()
+
+
+def autotune_table() -> str:
+    """The shape table as text (one ``kind stride rows_log2 degree_log2 g tiles variant`` per line)."""
+    need = ctypes.c_uint64()
+    _lib.check(_lib.lib().grgx_autotune_export(None, 0, ctypes.byref(need)))
+    buf = ctypes.create_string_buffer(int(need.value) + 1)
+    _lib.check(_lib.lib().grgx_autotune_export(buf, len(buf), ctypes.byref(need)))
+    return buf.value.decode()
+
+
+def autotune_load(text: str) -> None:
+    """Merge a saved shape table (``autotune_table()`` output) into the process-wide table."""
+    _lib.check(_lib.lib().grgx_autotune_import(text.encode()))
+
+
+def autotune_clear() -> None:
+    """Empty the shape table: every level runs its default shape."""
+    _lib.lib().grgx_autotune_clear()
+
+
 def matmul_batch(grg: GRG, requests, max_cols: int = 0, *, f32_compensated: bool = True, f64_native: bool = False):
     """Several products on one graph, coalesced into shared traversals.
 

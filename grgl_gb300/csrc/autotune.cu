@@ -1,0 +1,239 @@
+// Launch-shape autotuner for the level sweep.
+//
+// A level's sweep can run with G lanes per row (G = the default for the row's K, half or a
+// quarter of it -- fewer lanes per row means more rows per warp and more column tiles) and with
+// the default or the deep prefetch variant (twice the gathers in flight per lane, one block per
+// SM less).  Which is fastest depends on the level's width (rows), its mean degree (edges per
+// row) and K, so the table is keyed on
+//     (storage kind, row stride in elements, floor(log2(rows + 1)), floor(log2(edges / rows + 1)))
+// and filled by measuring: grgx_autotune times every candidate on each level of one traversal
+// of a resident graph (CUDA events around the level's launch, best of three) and records the
+// winner when it beats the default by more than 2%.  Calls on any graph then look up every
+// level's key; levels without an entry run the default shape.  Shapes change only the order in
+// which a row's float terms are added (integer results are bit-exact with any shape).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cstdio>
+#include <map>
+#include <mutex>
+#include <sstream>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "device_plan.h"
+
+namespace grgx {
+
+namespace {
+
+using Key = std::tuple<int, long long, int, int>;
+
+std::mutex g_table_mu;
+std::map<Key, LevelShape> g_table;
+std::atomic<bool> g_table_nonempty{false};
+
+int ilog2p1(long long x) {
+    int l = 0;
+    for (unsigned long long v = static_cast<unsigned long long>(x) + 1; v > 1; v >>= 1) l++;
+    return l;
+}
+
+Key key_for(const Layout& L, long long rows, long long edges) {
+    return Key{static_cast<int>(L.kind), L.stride, ilog2p1(rows), ilog2p1(rows > 0 ? edges / rows : 0)};
+}
+
+bool has_deep(const Layout& L) {
+    const bool kindOk = L.kind == Kind::U32 || L.kind == Kind::F32C || L.kind == Kind::F32 || L.kind == Kind::F64S;
+    return kindOk && L.vw * L.ssize == 16;
+}
+
+int tiles_for(const Layout& L, int g) {
+    const long long vecs = L.stride / L.vw;
+    return static_cast<int>((vecs + g - 1) / g);
+}
+
+// Candidate lane counts: the default and up to two halvings (each a compiled shape).
+std::vector<int> candidate_g(const Layout& L) {
+    std::vector<int> gs{L.g};
+    if (L.vw * L.ssize == 16) {
+        for (int g = L.g / 2; g >= 1 && gs.size() < 3; g /= 2) gs.push_back(g);
+    }
+    return gs;
+}
+
+bool valid_shape(const Layout& L, const LevelShape& s) {
+    if (s.variant != 0 && !has_deep(L)) return false;
+    const std::vector<int> gs = candidate_g(L);
+    return std::find(gs.begin(), gs.end(), s.g) != gs.end() && s.ntiles == tiles_for(L, s.g);
+}
+
+}  // namespace
+
+LevelShape default_shape(const Layout& L) { return LevelShape{L.g, L.ntiles, 0}; }
+
+int max_tiles(const Layout& L) {
+    int t = L.ntiles;
+    for (int g : candidate_g(L)) t = std::max(t, tiles_for(L, g));
+    return t;
+}
+
+LevelShape level_shape(const Layout& L, const DevCSR& c, size_t level) {
+    if (!g_table_nonempty.load(std::memory_order_acquire) || level >= c.level_rows.size()) return default_shape(L);
+    std::lock_guard<std::mutex> lk(g_table_mu);
+    auto it = g_table.find(key_for(L, c.level_rows[level], c.level_edges[level]));
+    if (it == g_table.end() || !valid_shape(L, it->second)) return default_shape(L);
+    return it->second;
+}
+
+void autotune_clear() {
+    std::lock_guard<std::mutex> lk(g_table_mu);
+    g_table.clear();
+    g_table_nonempty.store(false, std::memory_order_release);
+}
+
+// One line per entry: kind stride rows_log2 degree_log2 g ntiles variant.
+std::string autotune_export() {
+    std::lock_guard<std::mutex> lk(g_table_mu);
+    std::ostringstream os;
+    for (const auto& kv : g_table)
+        os << std::get<0>(kv.first) << ' ' << std::get<1>(kv.first) << ' ' << std::get<2>(kv.first) << ' '
+           << std::get<3>(kv.first) << ' ' << kv.second.g << ' ' << kv.second.ntiles << ' ' << kv.second.variant
+           << '\n';
+    return os.str();
+}
+
+void autotune_import(const std::string& text) {
+    std::istringstream is(text);
+    std::vector<std::pair<Key, LevelShape>> rows;
+    std::string line;
+    while (std::getline(is, line)) {
+        if (line.empty()) continue;
+        std::istringstream ls(line);
+        int kind = 0, rl = 0, dl = 0;
+        long long stride = 0;
+        LevelShape s;
+        GRGX_CHECK(static_cast<bool>(ls >> kind >> stride >> rl >> dl >> s.g >> s.ntiles >> s.variant), GRGX_ERR_API_MISUSE,
+                   "malformed autotune table line: " + line);
+        GRGX_CHECK(kind >= 0 && kind <= static_cast<int>(Kind::F64S) && stride > 0 && s.g >= 1 && s.g <= 32 &&
+                       (s.g & (s.g - 1)) == 0 && s.ntiles >= 1 && (s.variant == 0 || s.variant == 1),
+                   GRGX_ERR_API_MISUSE, "invalid autotune table entry: " + line);
+        rows.push_back({Key{kind, stride, rl, dl}, s});
+    }
+    std::lock_guard<std::mutex> lk(g_table_mu);
+    for (auto& r : rows) g_table[r.first] = r.second;
+    g_table_nonempty.store(!g_table.empty(), std::memory_order_release);
+}
+
+void clear_graph_replays(grgx_graph* g);
+
+// Times every candidate shape on each level of one traversal in `direction` and records the
+// winners.  The values swept are zeros: the gathers, the edge walk and the arithmetic do not
+// depend on them.
+std::string autotune_impl(grgx_graph* g, int dtype, uint64_t rows, int direction, uint32_t flags) {
+    GRGX_CHECK(dtype >= GRGX_F64 && dtype <= GRGX_BOOL, GRGX_ERR_API_MISUSE, "Unsupported dtype");
+    GRGX_CHECK(direction == GRGX_DIRECTION_DOWN || direction == GRGX_DIRECTION_UP, GRGX_ERR_API_MISUSE,
+               "Invalid traversal direction");
+    GRGX_CHECK(rows > 0 && rows <= 2000000ull, GRGX_ERR_API_MISUSE, "matmul() requires non-zero dimensions.");
+    DevicePlan* dp = ensure_device_plan(g);
+    const Layout L = choose_layout(dtype, static_cast<long long>(rows), (flags & GRGX_FLAG_F32_PLAIN) != 0,
+                                   (flags & GRGX_FLAG_F64_NATIVE) != 0);
+    const bool down = (direction == GRGX_DIRECTION_DOWN);
+    const DevCSR& c = down ? dp->down : dp->up;
+    const int maxT = max_tiles(L);
+    const size_t n = g->host->num_nodes;
+    cudaStream_t s = nullptr;
+    GRGX_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    void *vals = nullptr, *partials = nullptr;
+    unsigned* counters = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    std::ostringstream rep;
+    auto release = [&] {
+        if (vals) cudaFree(vals);
+        if (partials) cudaFree(partials);
+        if (counters) cudaFree(counters);
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        cudaStreamDestroy(s);
+    };
+    try {
+        const size_t valBytes = n * static_cast<size_t>(L.stride) * L.ssize;
+        GRGX_CUDA(cudaMalloc(&vals, std::max<size_t>(valBytes, 16)));
+        GRGX_CUDA(cudaMemsetAsync(vals, 0, valBytes, s));
+        GRGX_CUDA(cudaMalloc(&partials, std::max<size_t>(static_cast<size_t>(c.n_pieces) * L.stride * L.asize, 16)));
+        const size_t counterBytes = static_cast<size_t>(c.n_heavy + 1) * maxT * sizeof(unsigned);
+        GRGX_CUDA(cudaMalloc(&counters, counterBytes));
+        GRGX_CUDA(cudaEventCreate(&e0));
+        GRGX_CUDA(cudaEventCreate(&e1));
+        unsigned* tickets = counters;
+        unsigned* work = counters + c.n_heavy * maxT;
+        const int rmw = down ? 1 : 0;
+        auto time_shape = [&](size_t lvl, const LevelShape& sh) {
+            float best = 1e30f;
+            for (int rep_i = 0; rep_i < 4; rep_i++) {
+                GRGX_CUDA(cudaMemsetAsync(counters, 0, counterBytes, s));
+                GRGX_CUDA(cudaEventRecord(e0, s));
+                launch_level(L, c, lvl, vals, vals, rmw, partials, tickets, work, s, nullptr, 0, &sh, maxT);
+                GRGX_CUDA(cudaEventRecord(e1, s));
+                GRGX_CUDA(cudaEventSynchronize(e1));
+                GRGX_CUDA(cudaGetLastError());
+                float ms = 0;
+                GRGX_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+                if (rep_i > 0) best = std::min(best, ms);  // the first launch warms up
+            }
+            return best;
+        };
+        std::vector<LevelShape> cands;
+        for (int gg : candidate_g(L)) {
+            cands.push_back(LevelShape{gg, tiles_for(L, gg), 0});
+            if (has_deep(L)) cands.push_back(LevelShape{gg, tiles_for(L, gg), 1});
+        }
+        double totDefault = 0, totBest = 0;
+        for (size_t lvl = 0; lvl < c.lb.size(); lvl++) {
+            if (c.le[lvl] <= c.lb[lvl]) continue;
+            const LevelShape def = default_shape(L);
+            const float tDef = time_shape(lvl, def);
+            LevelShape best = def;
+            float tBest = tDef;
+            for (const LevelShape& sh : cands) {
+                if (sh.g == def.g && sh.variant == def.variant) continue;
+                const float t = time_shape(lvl, sh);
+                if (t < tBest) {
+                    tBest = t;
+                    best = sh;
+                }
+            }
+            if (tBest > 0.98f * tDef) {
+                best = def;
+                tBest = tDef;
+            }
+            totDefault += tDef;
+            totBest += tBest;
+            {
+                std::lock_guard<std::mutex> lk(g_table_mu);
+                g_table[key_for(L, c.level_rows[lvl], c.level_edges[lvl])] = best;
+                g_table_nonempty.store(true, std::memory_order_release);
+            }
+            char line[256];
+            std::snprintf(line, sizeof(line),
+                          "level %zu rows %lld edges %lld: g %d tiles %d variant %d, %.4f ms (default g %d variant "
+                          "0: %.4f ms)\n",
+                          lvl, c.level_rows[lvl], c.level_edges[lvl], best.g, best.ntiles, best.variant, tBest,
+                          def.g, tDef);
+            rep << line;
+        }
+        char tail[160];
+        std::snprintf(tail, sizeof(tail), "sweep %.4f ms tuned, %.4f ms default\n", totBest, totDefault);
+        rep << tail;
+    } catch (...) {
+        release();
+        throw;
+    }
+    release();
+    clear_graph_replays(g);
+    return rep.str();
+}
+
+}  // namespace grgx

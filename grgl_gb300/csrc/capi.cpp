@@ -1,5 +1,6 @@
 // The C ABI (include/grgx.h): exception-free wrappers over the host graph, the plan and the
 // matmul orchestration.
+#include <algorithm>
 #include <cstring>
 #include <string>
 
@@ -21,6 +22,10 @@ void matmul_batch_impl(grgx_graph* g, const grgx_request* reqs, uint64_t n, uint
                        void* stream);
 void matmul_standardized_impl(grgx_graph* g, int dtype, const void* input, uint64_t in_cols, uint64_t rows,
                               int direction, void* output, uint64_t output_size, uint32_t flags, void* stream);
+std::string autotune_impl(grgx_graph* g, int dtype, uint64_t rows, int direction, uint32_t flags);
+std::string autotune_export();
+void autotune_import(const std::string& text);
+void autotune_clear();
 
 namespace {
 thread_local std::string t_error;
@@ -300,6 +305,39 @@ grgx_status grgx_measure_l2_bandwidth(uint64_t bytes, int reps, double* gbps) {
         *gbps = measure_l2_bandwidth(bytes, reps);
     });
 }
+
+namespace {
+// Copies `text` (NUL-terminated, truncated to `len`) and reports the size it needs.
+void copy_text(const std::string& text, char* buf, uint64_t len, uint64_t* needed) {
+    if (needed) *needed = text.size() + 1;
+    if (buf && len > 0) {
+        const size_t k = std::min<size_t>(text.size(), static_cast<size_t>(len - 1));
+        std::memcpy(buf, text.data(), k);
+        buf[k] = '\0';
+    }
+}
+}  // namespace
+
+grgx_status grgx_autotune(grgx_graph* g, grgx_dtype dtype, uint64_t rows, grgx_direction direction, uint32_t flags,
+                          char* report, uint64_t report_len, uint64_t* report_needed) {
+    return guarded([&] {
+        GRGX_CHECK(g, GRGX_ERR_API_MISUSE, "null argument");
+        copy_text(autotune_impl(g, dtype, rows, direction, flags), report, report_len, report_needed);
+    });
+}
+
+grgx_status grgx_autotune_export(char* buf, uint64_t len, uint64_t* needed) {
+    return guarded([&] { copy_text(autotune_export(), buf, len, needed); });
+}
+
+grgx_status grgx_autotune_import(const char* text) {
+    return guarded([&] {
+        GRGX_CHECK(text, GRGX_ERR_API_MISUSE, "null argument");
+        autotune_import(text);
+    });
+}
+
+void grgx_autotune_clear(void) { autotune_clear(); }
 
 void grgx_set_timing(int enabled) { set_timing(enabled); }
 

@@ -26,6 +26,7 @@ struct DevCSR {
     ChunkDev* chunks = nullptr;
     HeavyDev* heavy = nullptr;
     std::vector<int32_t> lb, le;
+    std::vector<long long> level_rows, level_edges;  // per level, for the launch-shape table
     long long n_heavy = 0, n_pieces = 0, n_edges = 0, n_rows = 0;
 };
 
@@ -55,16 +56,32 @@ struct Layout {
     int vw, g, ntiles;
 };
 
-// Element layout of one call: storage kind, row stride and the (VW, G) sweep shape.
+// Element layout of one call: storage kind, row stride and the default (VW, G) sweep shape.
 Layout choose_layout(int dtype, long long K, bool plainF32, bool nativeF64);
+
+// Launch shape of one level: G lanes per row, the column tiles that G leaves (the K-tile
+// count), and the prefetch-depth variant (0 default, 1 deep).
+struct LevelShape {
+    int g = 1;
+    int ntiles = 1;
+    int variant = 0;
+};
+LevelShape default_shape(const Layout& L);
+// The shape a level runs with: the autotuner's entry for (storage kind, row stride, the level's
+// width and mean degree) when there is one, else the default.
+LevelShape level_shape(const Layout& L, const DevCSR& c, size_t level);
+// Column tiles of the widest shape the autotuner may pick for L: the stride of the per-launch
+// work counters and of the heavy-row tickets.
+int max_tiles(const Layout& L);
 
 int sm_count();
 
 // Launches one level of a CSR (a no-op when the level has no chunks); `work` points at
-// L.ntiles zeroed counters owned by this launch.  Returns the number of kernels launched.
+// `tileStride` (0: L.ntiles) zeroed counters owned by this launch, and the heavy-row tickets
+// are `tileStride` apart.  `shape` null: the default shape.  Returns the kernels launched.
 int launch_level(const Layout& L, const DevCSR& c, size_t level, const void* src, void* dst, int rmw,
                  void* partials, unsigned* tickets, unsigned* work, cudaStream_t s, const int* gate = nullptr,
-                 int gateValue = 0);
+                 int gateValue = 0, const LevelShape* shape = nullptr, int tileStride = 0);
 
 // Builds (once) and returns the graph's plan on the current device.
 DevicePlan* ensure_device_plan(grgx_graph* g);

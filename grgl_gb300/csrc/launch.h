@@ -11,14 +11,23 @@ namespace grgx {
 // Storage/accumulation kinds (see ops.cuh).
 enum class Kind { U32, U64, F64, F32C, F32, XOR, F64S };
 
-// One level (or seed pass) of the sweep; VW elements per lane, G lanes per row.
-void launch_sweep_u32(const SweepParams<uint32_t>& p, int vw, int g, dim3 grid, int sms, cudaStream_t s);
-void launch_sweep_xor(const SweepParams<uint32_t>& p, int vw, int g, dim3 grid, int sms, cudaStream_t s);
-void launch_sweep_u64(const SweepParams<unsigned long long>& p, int vw, int g, dim3 grid, int sms, cudaStream_t s);
-void launch_sweep_f64(const SweepParams<double>& p, int vw, int g, dim3 grid, int sms, cudaStream_t s);
-void launch_sweep_f32c(const SweepParams<float>& p, int vw, int g, dim3 grid, int sms, cudaStream_t s);
-void launch_sweep_f32(const SweepParams<float>& p, int vw, int g, dim3 grid, int sms, cudaStream_t s);
-void launch_sweep_f64s(const SweepParams<DF>& p, int vw, int g, dim3 grid, int sms, cudaStream_t s);
+// One level (or seed pass) of the sweep; VW elements per lane, G lanes per row, `variant` 0 for
+// the default depth or 1 for the deep variant (float32, compensated float32, int32 and
+// float-pair float64 storage only).
+void launch_sweep_u32(const SweepParams<uint32_t>& p, int vw, int g, int variant, dim3 grid,
+                      int sms, cudaStream_t s);
+void launch_sweep_xor(const SweepParams<uint32_t>& p, int vw, int g, int variant, dim3 grid,
+                      int sms, cudaStream_t s);
+void launch_sweep_u64(const SweepParams<unsigned long long>& p, int vw, int g, int variant, dim3 grid,
+                      int sms, cudaStream_t s);
+void launch_sweep_f64(const SweepParams<double>& p, int vw, int g, int variant, dim3 grid,
+                      int sms, cudaStream_t s);
+void launch_sweep_f32c(const SweepParams<float>& p, int vw, int g, int variant, dim3 grid,
+                      int sms, cudaStream_t s);
+void launch_sweep_f32(const SweepParams<float>& p, int vw, int g, int variant, dim3 grid,
+                      int sms, cudaStream_t s);
+void launch_sweep_f64s(const SweepParams<DF>& p, int vw, int g, int variant, dim3 grid,
+                      int sms, cudaStream_t s);
 
 // Column-map modes of the transposing loads/stores.
 enum MapMode { MAP_IDENT = 0, MAP_DIV = 1, MAP_TABLE = 2, MAP_FOLD = 3 };

@@ -60,6 +60,12 @@ DevCSR upload_csr(DevicePlan& d, const PullCSR& c) {
     r.n_pieces = c.num_pieces;
     r.n_edges = c.num_edges;
     r.n_rows = static_cast<long long>(c.rows.size());
+    for (size_t l = 0; l < c.level_chunk_begin.size(); l++) {
+        const Chunk& a = c.chunks[static_cast<size_t>(c.level_chunk_begin[l])];
+        const Chunk& b = c.chunks[static_cast<size_t>(c.level_chunk_end[l])];
+        r.level_rows.push_back(static_cast<long long>(b.r0) - a.r0);
+        r.level_edges.push_back(static_cast<long long>(b.e0 - a.e0));
+    }
     return r;
 }
 
@@ -171,45 +177,30 @@ SweepParams<S> make_params(const DevCSR& c, long long cb, long long ce, const vo
 // `work` points at L.ntiles zeroed counters owned by this launch.
 int launch_level(const Layout& L, const DevCSR& c, size_t level, const void* src, void* dst, int rmw,
                  void* partials, unsigned* tickets, unsigned* work, cudaStream_t s, const int* gate,
-                 int gateValue) {
+                 int gateValue, const LevelShape* shape, int tileStride) {
     const long long cb = c.lb[level], ce = c.le[level];
     if (ce <= cb) return 0;
-    const dim3 grid(static_cast<unsigned>((ce - cb + 7) / 8), static_cast<unsigned>(L.ntiles));
+    const LevelShape sh = shape ? *shape : default_shape(L);
+    const int ts = tileStride > 0 ? tileStride : L.ntiles;
+    if (sh.ntiles > ts) throw Error(GRGX_ERR_CUDA, "launch shape has more column tiles than counters");
+    const dim3 grid(static_cast<unsigned>((ce - cb + 7) / 8), static_cast<unsigned>(sh.ntiles));
     const int sms = sm_count();
-    auto gated = [&](auto p) {
+    auto prm = [&](auto tag) {
+        using S = decltype(tag);
+        SweepParams<S> p = make_params<S>(c, cb, ce, src, dst, L.stride, rmw, partials, tickets, work, ts);
         p.gate = gate;
         p.gate_value = gateValue;
         return p;
     };
+    const int vw = L.vw, g = sh.g, v = sh.variant;
     switch (L.kind) {
-    case Kind::U32:
-        launch_sweep_u32(gated(make_params<uint32_t>(c, cb, ce, src, dst, L.stride, rmw, partials, tickets, work, L.ntiles)),
-                         L.vw, L.g, grid, sms, s);
-        break;
-    case Kind::XOR:
-        launch_sweep_xor(gated(make_params<uint32_t>(c, cb, ce, src, dst, L.stride, rmw, partials, tickets, work, L.ntiles)),
-                         L.vw, L.g, grid, sms, s);
-        break;
-    case Kind::U64:
-        launch_sweep_u64(gated(make_params<unsigned long long>(c, cb, ce, src, dst, L.stride, rmw, partials, tickets, work, L.ntiles)), L.vw,
-            L.g, grid, sms, s);
-        break;
-    case Kind::F64:
-        launch_sweep_f64(gated(make_params<double>(c, cb, ce, src, dst, L.stride, rmw, partials, tickets, work, L.ntiles)),
-                         L.vw, L.g, grid, sms, s);
-        break;
-    case Kind::F32C:
-        launch_sweep_f32c(gated(make_params<float>(c, cb, ce, src, dst, L.stride, rmw, partials, tickets, work, L.ntiles)),
-                          L.vw, L.g, grid, sms, s);
-        break;
-    case Kind::F32:
-        launch_sweep_f32(gated(make_params<float>(c, cb, ce, src, dst, L.stride, rmw, partials, tickets, work, L.ntiles)),
-                         L.vw, L.g, grid, sms, s);
-        break;
-    case Kind::F64S:
-        launch_sweep_f64s(gated(make_params<DF>(c, cb, ce, src, dst, L.stride, rmw, partials, tickets, work, L.ntiles)),
-                          L.vw, L.g, grid, sms, s);
-        break;
+    case Kind::U32: launch_sweep_u32(prm(uint32_t{}), vw, g, v, grid, sms, s); break;
+    case Kind::XOR: launch_sweep_xor(prm(uint32_t{}), vw, g, v, grid, sms, s); break;
+    case Kind::U64: launch_sweep_u64(prm(static_cast<unsigned long long>(0)), vw, g, v, grid, sms, s); break;
+    case Kind::F64: launch_sweep_f64(prm(double{}), vw, g, v, grid, sms, s); break;
+    case Kind::F32C: launch_sweep_f32c(prm(float{}), vw, g, v, grid, sms, s); break;
+    case Kind::F32: launch_sweep_f32(prm(float{}), vw, g, v, grid, sms, s); break;
+    case Kind::F64S: launch_sweep_f64s(prm(DF{}), vw, g, v, grid, sms, s); break;
     }
     return 1;
 }
@@ -384,10 +375,12 @@ void matmul_direct(grgx_graph* g, int dtype, const void* input, uint64_t in_cols
         const long long nh = down ? (dp->down.n_heavy + dp->seed.n_heavy + dp->miss.n_heavy) : dp->up.n_heavy;
         const long long nslots = down ? (2 + static_cast<long long>(dp->down.lb.size()))
                                       : static_cast<long long>(dp->up.lb.size());
-        const size_t counterBytes = static_cast<size_t>(nh + nslots) * L.ntiles * sizeof(unsigned);
+        // counters per launch and per heavy row: enough column tiles for any launch shape
+        const int TS = max_tiles(L);
+        const size_t counterBytes = static_cast<size_t>(nh + nslots) * TS * sizeof(unsigned);
         unsigned* tickets = static_cast<unsigned*>(sc.get(counterBytes));
         GRGX_CUDA(cudaMemsetAsync(tickets, 0, counterBytes, s));
-        unsigned* work = tickets + nh * L.ntiles;  // one set of L.ntiles counters per launch
+        unsigned* work = tickets + nh * TS;  // one set of TS counters per launch
 
         // ---- float64: row scales and the device-side choice between the float-pair path (gate
         // 0) and the FP64-pipe path (gate 1, for rows spanning too many binades) ---------------
@@ -451,7 +444,8 @@ void matmul_direct(grgx_graph* g, int dtype, const void* input, uint64_t in_cols
                 launches++;
             };
             auto level = [&](const DevCSR& c, size_t lvl, const void* src, int rmw, unsigned* tk, unsigned* wk) {
-                return launch_level(LL, c, lvl, src, vals, rmw, partials, tk, wk, s, g, gv);
+                const LevelShape sh = level_shape(LL, c, lvl);
+                return launch_level(LL, c, lvl, src, vals, rmw, partials, tk, wk, s, g, gv, &sh, TS);
             };
             switch (init_kind) {
             case GRGX_INIT_VECTOR:
@@ -478,15 +472,15 @@ void matmul_direct(grgx_graph* g, int dtype, const void* input, uint64_t in_cols
                     load_rows(dIn, in_cols, M, MAP_IDENT, 1, nullptr, vt, 0);
                     launches += level(dp->seed, 0, vt, hasInit, tk, work);
                 }
-                tk += dp->seed.n_heavy * LL.ntiles;
+                tk += dp->seed.n_heavy * TS;
                 if (mt) {
                     load_rows(dMiss, M, M, MAP_IDENT, 1, nullptr, mt, 0);
-                    launches += level(dp->miss, 0, mt, 1, tk, work + LL.ntiles);
+                    launches += level(dp->miss, 0, mt, 1, tk, work + TS);
                 }
-                tk += dp->miss.n_heavy * LL.ntiles;
+                tk += dp->miss.n_heavy * TS;
                 if (timed && t_timing) GRGX_CUDA(cudaEventRecord(ev[1], s));
                 for (size_t lvl = 0; lvl < dp->down.lb.size(); lvl++)
-                    launches += level(dp->down, lvl, vals, 1, tk, work + (2 + lvl) * LL.ntiles);
+                    launches += level(dp->down, lvl, vals, 1, tk, work + (2 + lvl) * TS);
                 if (timed && t_timing) GRGX_CUDA(cudaEventRecord(ev[2], s));
                 if (emit_all) {
                     store_cols(n, MAP_TABLE, 1, dp->old2new, dOut, out_cols, add);
@@ -500,7 +494,7 @@ void matmul_direct(grgx_graph* g, int dtype, const void* input, uint64_t in_cols
                 load_rows(dIn, in_cols, N, by_indiv ? MAP_DIV : MAP_IDENT, P, nullptr, vals, hasInit);
                 if (timed && t_timing) GRGX_CUDA(cudaEventRecord(ev[1], s));
                 for (size_t lvl = 0; lvl < dp->up.lb.size(); lvl++)
-                    launches += level(dp->up, lvl, vals, hasInit, tickets, work + lvl * LL.ntiles);
+                    launches += level(dp->up, lvl, vals, hasInit, tickets, work + lvl * TS);
                 if (timed && t_timing) GRGX_CUDA(cudaEventRecord(ev[2], s));
                 if (emit_all) {
                     store_cols(n, MAP_TABLE, 1, dp->old2new, dOut, out_cols, add);
@@ -682,6 +676,11 @@ void matmul_impl(grgx_graph* g, int dtype, const void* input, uint64_t in_cols, 
     } else {
         GRGX_CUDA(cudaStreamSynchronize(e->stream));
     }
+}
+
+void clear_graph_replays(grgx_graph* g) {
+    std::lock_guard<std::mutex> lk(g->mu);
+    g->graphs.reset();
 }
 
 void set_timing(int enabled) { t_timing = enabled != 0; }

@@ -125,14 +125,14 @@ template <> struct ChainTraits<AddF64S> {
     static constexpr bool kChains = true;
 };
 
-template <class Op, int VW, int G>
+template <class Op, int VW, int G, int D>
 __device__ __forceinline__ void sweep_chunk(const SweepParams<typename Op::S>& p, long long c, int lane) {
     using S = typename Op::S;
     using A = typename Op::A;
     using Acc = VecAcc<Op, VW>;
     constexpr int NG = 32 / G;  // groups per warp = edges per sub-step
-    // gathers in flight per lane: 4 for 16-byte vectors, 8 for narrower ones
-    constexpr int BATCH = (VW * sizeof(S) >= 16) ? 4 : 8;
+    // gathers in flight per lane: 4 for 16-byte vectors, 8 for narrower ones, times the depth D
+    constexpr int BATCH = ((VW * sizeof(S) >= 16) ? 4 : 8) * D;
     constexpr int UNR = (G >= BATCH) ? 1 : BATCH / G;  // 32-edge blocks per step
     constexpr int STEPS = UNR * G;                     // sub-steps per step (a multiple of BATCH)
     constexpr unsigned NGMASK = (NG == 32) ? 0xffffffffu : ((1u << NG) - 1u);
@@ -293,14 +293,16 @@ __device__ __forceinline__ void sweep_chunk(const SweepParams<typename Op::S>& p
 // Persistent warps: each warp takes chunks of the level from a shared counter until none are
 // left, so long and short chunks balance across the SMs.
 // Blocks per SM the register budget is sized for (65536 / (256 * blocks) registers per thread).
-template <class Op, int VW, int G> struct SweepOccupancy {
+// The deep variant (D = 2) keeps twice the gathers in flight per lane and gives up one block
+// per SM for the registers they take; which of the two a level runs is the autotuner's choice.
+template <class Op, int VW, int G, int D> struct SweepOccupancy {
     // compensated float shapes with several 32-edge blocks per step hold more state per lane
     static constexpr bool kWide = (std::is_same<Op, AddF32C>::value || std::is_same<Op, AddF64S>::value) && G <= 2 && VW >= 2;
-    static constexpr int kBlocks = kWide ? 3 : 4;
+    static constexpr int kBlocks = (kWide ? 3 : 4) - (D > 1 ? 1 : 0);
 };
 
-template <class Op, int VW, int G>
-__global__ void __launch_bounds__(256, SweepOccupancy<Op, VW, G>::kBlocks) sweep_kernel(const SweepParams<typename Op::S> p) {
+template <class Op, int VW, int G, int D>
+__global__ void __launch_bounds__(256, SweepOccupancy<Op, VW, G, D>::kBlocks) sweep_kernel(const SweepParams<typename Op::S> p) {
     if (p.gate != nullptr && *p.gate != p.gate_value) return;
     const int lane = threadIdx.x & 31;
     unsigned* counter = p.work + blockIdx.y;
@@ -309,7 +311,7 @@ __global__ void __launch_bounds__(256, SweepOccupancy<Op, VW, G>::kBlocks) sweep
         if (lane == 0) c = (long long)atomicAdd(counter, 1u);
         c = __shfl_sync(FULL_MASK, c, 0) + p.c_begin;
         if (c >= p.c_end) return;
-        sweep_chunk<Op, VW, G>(p, c, lane);
+        sweep_chunk<Op, VW, G, D>(p, c, lane);
     }
 }
 

@@ -239,6 +239,29 @@ grgx_status grgx_matmul_noalloc(grgx_graph* g, grgx_dtype dtype, const void* inp
  * ceiling of the sweep's row gathers when the gathered rows stay in L2. */
 grgx_status grgx_measure_l2_bandwidth(uint64_t bytes, int reps, double* gbps);
 
+/* ---- launch-shape autotuner -------------------------------------------------------------
+ * No counterpart in the reference.  Each level of the sweep can run with G lanes per row (the
+ * default for its K, half or a quarter of it: more rows per warp, more column tiles) and with
+ * the default or a deep prefetch variant (twice the gathers in flight per lane).  The
+ * process-wide table is keyed on (storage kind, row stride, log2 of the level's rows, log2 of
+ * its mean degree); levels without an entry run the default shape.
+ *
+ * grgx_autotune times every candidate on each level of one traversal of `g` (resident on the
+ * current device; it is uploaded first) for `rows` x cols inputs of `dtype` in `direction`
+ * (`flags`: GRGX_FLAG_F32_PLAIN / GRGX_FLAG_F64_NATIVE select the accumulator as in
+ * grgx_matmul), records each level's winner when it beats the default by more than 2%, and
+ * writes a per-level report to `report` (NUL-terminated, truncated to `report_len`;
+ * `report_needed`, if not NULL, gets the full size).  It drops `g`'s captured CUDA graphs; make
+ * no other call on `g` while it runs.  Float results may round differently under another shape
+ * (the order of a row's terms changes); integer results do not change. */
+grgx_status grgx_autotune(grgx_graph* g, grgx_dtype dtype, uint64_t rows, grgx_direction direction, uint32_t flags,
+                          char* report, uint64_t report_len, uint64_t* report_needed);
+/* The table as text, one entry per line ("kind stride rows_log2 degree_log2 g tiles variant"),
+ * for saving; import merges such text back (entries invalid for a shape are ignored at use). */
+grgx_status grgx_autotune_export(char* buf, uint64_t len, uint64_t* needed);
+grgx_status grgx_autotune_import(const char* text);
+void grgx_autotune_clear(void);
+
 /* Device-time breakdown of the last grgx_matmul made by this thread with timing enabled. */
 typedef struct {
     float total_ms;     /* seed + sweep + gather, CUDA events */
