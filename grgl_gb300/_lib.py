@@ -64,6 +64,8 @@ SIGNATURES = {
     "grgx_server_wait": (_int, [_vp, _u64, ctypes.c_double, ctypes.POINTER(RequestStats)]),
     "grgx_server_destroy": (None, [_vp]),
     "grgx_measure_l2_bandwidth": (_int, [_u64, _int, ctypes.POINTER(ctypes.c_double)]),
+    "grgx_host_alloc": (_int, [_u64, ctypes.POINTER(_vp)]),
+    "grgx_host_free": (None, [_vp]),
     "grgx_autotune": (_int, [c_graph_p, _int, _u64, _int, _u32, ctypes.c_char_p, _u64, ctypes.POINTER(_u64)]),
     "grgx_autotune_export": (_int, [ctypes.c_char_p, _u64, ctypes.POINTER(_u64)]),
     "grgx_autotune_import": (_int, [ctypes.c_char_p]),

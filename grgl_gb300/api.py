@@ -221,6 +221,39 @@ def _flags(f32_compensated: bool, f64_native: bool) -> int:
             | (0 if _GRAPHS_ENABLED[0] else _lib.FLAG_NO_GRAPH))
 
 
+_PINNED_MIN_BYTES = 4 << 20
+
+
+class _PinnedBlock:
+    """Owner of one pinned host block from libgrgx's pool; returns it when collected."""
+
+    __slots__ = ("ptr",)
+
+    def __init__(self, ptr):
+        self.ptr = ptr
+
+    def __del__(self):
+        try:
+            _lib.lib().grgx_host_free(self.ptr)
+        except Exception:  # interpreter shutdown
+            pass
+
+
+def _host_empty(shape, dtype):
+    """An uninitialised host array for a result: pinned (pooled) memory when it is large, so
+    the device-to-host copy into it runs at full speed; plain numpy memory otherwise."""
+    dtype = np.dtype(dtype)
+    nbytes = int(np.prod(shape)) * dtype.itemsize
+    if nbytes < _PINNED_MIN_BYTES:
+        return np.empty(shape, dtype=dtype)
+    ptr = ctypes.c_void_p()
+    if _lib.lib().grgx_host_alloc(nbytes, ctypes.byref(ptr)) != _lib.OK:
+        return np.empty(shape, dtype=dtype)
+    buf = (ctypes.c_char * nbytes).from_address(ptr.value)
+    buf.owner = _PinnedBlock(ptr.value)
+    return np.frombuffer(buf, dtype=dtype).reshape(shape)
+
+
 def matmul(grg: GRG, input, direction, emit_all_nodes: bool = False, by_individual: bool = False, init=None,
            miss=None, *, f32_compensated: bool = True, f64_native: bool = False):
     """pygrgl.matmul on the GPU (reference: _grgl.cpp:187-241, grg.h:1341-1517).
@@ -245,7 +278,7 @@ def matmul(grg: GRG, input, direction, emit_all_nodes: bool = False, by_individu
     out_cols = grg.num_nodes if emit_all_nodes else (nsamp if direction == DOWN else grg.num_mutations)
     init_kind, init_arr = _parse_init(grg, init, arr.dtype, rows, code == 10)
     miss_arr = _parse_miss(miss, arr.dtype, rows, cols, out_cols, direction, emit_all_nodes)
-    out = np.empty((rows, out_cols), dtype=arr.dtype)
+    out = _host_empty((rows, out_cols), arr.dtype)
     flags = _lib.FLAG_OVERWRITE | _flags(f32_compensated, f64_native)
     _lib.check(_lib.lib().grgx_matmul(grg._h, code, arr.ctypes.data, cols, rows, int(direction), out.ctypes.data,
                                       out.size, int(bool(emit_all_nodes)), int(bool(by_individual)),
@@ -390,7 +423,7 @@ def matmul_standardized(grg: GRG, input, direction, *, f32_compensated: bool = T
     x = np.ascontiguousarray(input)
     _check(x.ndim == 2, "matmul() only support two dimensional numpy arrays as input.")
     _check(x.dtype in (np.float32, np.float64), "standardized products take float32 or float64 input")
-    out = np.empty((x.shape[0], rows_out), dtype=x.dtype)
+    out = _host_empty((x.shape[0], rows_out), x.dtype)
     _lib.check(_lib.lib().grgx_matmul_standardized(grg._h, 0 if x.dtype == np.float64 else 1, x.ctypes.data,
                                                    x.shape[1], x.shape[0], int(direction), out.ctypes.data,
                                                    out.size, flags, None))
@@ -430,7 +463,7 @@ def _request_for(grg, x, direction, standardized=False):
            else "Input vector is not size M (numMutations)")
     if standardized:
         _check(x.dtype in (np.float32, np.float64), "standardized products take float32 or float64 input")
-    out = np.empty((x.shape[0], out_cols), dtype=x.dtype)
+    out = _host_empty((x.shape[0], out_cols), x.dtype)
     return x, out, _lib.Request(_DTYPE_CODES[x.dtype], int(direction), x.shape[0], x.ctypes.data, out.ctypes.data,
                                 opts)
 

@@ -22,6 +22,8 @@ void matmul_batch_impl(grgx_graph* g, const grgx_request* reqs, uint64_t n, uint
                        void* stream);
 void matmul_standardized_impl(grgx_graph* g, int dtype, const void* input, uint64_t in_cols, uint64_t rows,
                               int direction, void* output, uint64_t output_size, uint32_t flags, void* stream);
+void* host_alloc(uint64_t bytes);
+void host_free(void* b);
 std::string autotune_impl(grgx_graph* g, int dtype, uint64_t rows, int direction, uint32_t flags);
 std::string autotune_export();
 void autotune_import(const std::string& text);
@@ -338,6 +340,15 @@ grgx_status grgx_autotune_import(const char* text) {
 }
 
 void grgx_autotune_clear(void) { autotune_clear(); }
+
+grgx_status grgx_host_alloc(uint64_t bytes, void** out) {
+    return guarded([&] {
+        GRGX_CHECK(out, GRGX_ERR_API_MISUSE, "null argument");
+        *out = host_alloc(bytes);
+    });
+}
+
+void grgx_host_free(void* p) { host_free(p); }
 
 void grgx_set_timing(int enabled) { set_timing(enabled); }
 

@@ -239,6 +239,14 @@ grgx_status grgx_matmul_noalloc(grgx_graph* g, grgx_dtype dtype, const void* inp
  * ceiling of the sweep's row gathers when the gathered rows stay in L2. */
 grgx_status grgx_measure_l2_bandwidth(uint64_t bytes, int reps, double* gbps);
 
+/* No counterpart in the reference.  Page-locked host memory for results the caller will have
+ * copied back (grgx_matmul / batch / server outputs in host memory): device-to-host copies
+ * into it run at the link's full speed, while a freshly allocated pageable buffer pays a page
+ * fault per page during the copy.  Freed blocks are cached by power-of-two size (16 GiB in
+ * all) for later calls.  grgx_host_free ignores pointers it did not hand out. */
+grgx_status grgx_host_alloc(uint64_t bytes, void** out);
+void grgx_host_free(void* p);
+
 /* ---- launch-shape autotuner -------------------------------------------------------------
  * No counterpart in the reference.  Each level of the sweep can run with G lanes per row (the
  * default for its K, half or a quarter of it: more rows per warp, more column tiles) and with
