@@ -515,13 +515,24 @@ def main():
     d2h = sum(K * (stats["mutations"] if d == UP else stats["samples"]) * dt.itemsize for dt, K, d in combos)
     e2e_value = None
     if not args.no_e2e:
+        # inputs in pinned host memory; one untimed step warms the library's pinned result pool
+        from grgl_gb300.api import _host_empty
+
+        pinned_inputs = []
+        for V in host_inputs:
+            P = _host_empty(V.shape, V.dtype)
+            P[...] = V
+            pinned_inputs.append(P)
+        step(pinned_inputs, None)
+        barrier()
         t0 = time.perf_counter()
         e2e_steps = max(1, min(args.steps, 2))
         for _ in range(e2e_steps):
-            step(host_inputs, None)
+            step(pinned_inputs, None)
         barrier()
         e2e_s = time.perf_counter() - t0
         e2e_value = units_per_step * e2e_steps * world / e2e_s
+        del pinned_inputs
 
     batched = serve = large = None
     if rank == 0 and not args.no_serve:
