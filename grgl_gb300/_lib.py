@@ -58,6 +58,7 @@ SIGNATURES = {
     "grgx_matmul_noalloc": (_int, [c_graph_p, _int, _vp, _u64, _u64, _int, _vp, _u64, _vp]),
     "grgx_matmul_batch": (_int, [c_graph_p, ctypes.POINTER(Request), _u64, _u64, _u32, _vp]),
     "grgx_matmul_standardized": (_int, [c_graph_p, _int, _vp, _u64, _u64, _int, _vp, _u64, _u32, _vp]),
+    "grgx_matmul_gram": (_int, [c_graph_p, _int, _vp, _u64, _u64, _int, _vp, _u64, _int, _u32, _vp]),
     "grgx_server_create": (_int, [_u32, _u64, _u64, ctypes.POINTER(_vp)]),
     "grgx_server_add_graph": (_int, [_vp, c_graph_p, ctypes.POINTER(_u32)]),
     "grgx_server_submit": (_int, [_vp, _u32, ctypes.POINTER(Request), ctypes.POINTER(_u64)]),

@@ -430,6 +430,36 @@ def matmul_standardized(grg: GRG, input, direction, *, f32_compensated: bool = T
     return out
 
 
+def matmul_gram(grg: GRG, input, first_direction, *, standardized: bool = False, f32_compensated: bool = True,
+                f64_native: bool = False):
+    """Two chained traversals with the intermediate kept on the GPU: ``V X X^T`` (first UP, V:
+    K x N) or ``V X^T X`` (first DOWN, V: K x M); with ``standardized`` the standardized Z
+    replaces X.  numpy in -> numpy out, CUDA tensor in -> CUDA tensor out."""
+    first = TraversalDirection(int(first_direction))
+    flags = _flags(f32_compensated, f64_native)
+    if _is_torch_cuda(input):
+        import torch
+
+        x = input.contiguous()
+        npd = _torch_dtype_to_np(x.dtype)
+        _check(x.dim() == 2 and npd is not None, "matmul() only support two dimensional numpy arrays as input.")
+        out = torch.empty_like(x)
+        stream = torch.cuda.current_stream(x.device).cuda_stream
+        _lib.check(_lib.lib().grgx_matmul_gram(grg._h, _DTYPE_CODES[np.dtype(npd)], x.data_ptr(), x.shape[1],
+                                               x.shape[0], int(first), out.data_ptr(), out.numel(),
+                                               int(bool(standardized)), flags | _lib.FLAG_DEVICE_POINTERS, stream))
+        return out
+    _check(isinstance(input, np.ndarray), f"Unsupported numpy dtype: {np.asarray(input).dtype}")
+    x = np.ascontiguousarray(input)
+    _check(x.ndim == 2, "matmul() only support two dimensional numpy arrays as input.")
+    _check(x.dtype in _DTYPE_CODES, f"Unsupported numpy dtype: {x.dtype}")
+    out = _host_empty(x.shape, x.dtype)
+    _lib.check(_lib.lib().grgx_matmul_gram(grg._h, _DTYPE_CODES[x.dtype], x.ctypes.data, x.shape[1], x.shape[0],
+                                           int(first), out.ctypes.data, out.size, int(bool(standardized)), flags,
+                                           None))
+    return out
+
+
 # ---- batching and serving ----------------------------------------------------------------------
 
 

@@ -22,6 +22,8 @@ void matmul_batch_impl(grgx_graph* g, const grgx_request* reqs, uint64_t n, uint
                        void* stream);
 void matmul_standardized_impl(grgx_graph* g, int dtype, const void* input, uint64_t in_cols, uint64_t rows,
                               int direction, void* output, uint64_t output_size, uint32_t flags, void* stream);
+void matmul_gram_impl(grgx_graph* g, int dtype, const void* input, uint64_t in_cols, uint64_t rows, int first,
+                      void* output, uint64_t output_size, int standardized, uint32_t flags, void* stream);
 void* host_alloc(uint64_t bytes);
 void host_free(void* b);
 std::string autotune_impl(grgx_graph* g, int dtype, uint64_t rows, int direction, uint32_t flags);
@@ -340,6 +342,16 @@ grgx_status grgx_autotune_import(const char* text) {
 }
 
 void grgx_autotune_clear(void) { autotune_clear(); }
+
+grgx_status grgx_matmul_gram(grgx_graph* g, grgx_dtype dtype, const void* input, uint64_t input_cols,
+                             uint64_t input_rows, grgx_direction first, void* output, uint64_t output_size,
+                             int standardized, uint32_t flags, void* stream) {
+    return guarded([&] {
+        GRGX_CHECK(g && input && output, GRGX_ERR_API_MISUSE, "null argument");
+        matmul_gram_impl(g, dtype, input, input_cols, input_rows, first, output, output_size, standardized, flags,
+                         stream);
+    });
+}
 
 grgx_status grgx_host_alloc(uint64_t bytes, void** out) {
     return guarded([&] {

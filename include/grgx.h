@@ -160,6 +160,15 @@ grgx_status grgx_matmul_standardized(grgx_graph* g, grgx_dtype dtype, const void
                                      uint64_t input_rows, grgx_direction direction, void* output,
                                      uint64_t output_size, uint32_t flags, void* stream);
 
+/* No counterpart in the reference (grapp's XX^T-style LinearOperators chain two matmul calls
+ * through host memory).  Two traversals chained on the device, the intermediate resident:
+ *   first = UP:   out = V X X^T  (V, out: K x N)     first = DOWN: out = V X^T X  (V, out: K x M)
+ * With `standardized` nonzero, Z (as grgx_matmul_standardized) replaces X (float32/float64).
+ * Flags as grgx_matmul_standardized; the output is overwritten. */
+grgx_status grgx_matmul_gram(grgx_graph* g, grgx_dtype dtype, const void* input, uint64_t input_cols,
+                             uint64_t input_rows, grgx_direction first, void* output, uint64_t output_size,
+                             int standardized, uint32_t flags, void* stream);
+
 /* One request of a batch or of the server: the plain product (no init, miss, emit_all_nodes or
  * by_individual) of `rows` x cols `input` in `direction`, written to `output` (rows x out_cols,
  * overwritten).  Host or device memory as the call's flags say.  With

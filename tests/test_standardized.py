@@ -94,3 +94,31 @@ def test_standardized_requests_batched_and_served(env):
                 assert np.all(np.abs(got.astype(np.float64) - ref) <= rtol * scale + 1e-300)
     with pytest.raises(RuntimeError, match="float32 or float64"):
         gx.matmul_batch(g, [(np.ones((1, g.num_samples), dtype=np.int32), UP, True)])
+
+
+@pytest.mark.parametrize("standardized", [False, True])
+def test_gram_products_match_dense(env, standardized):
+    """V X X^T / V X^T X (and with Z) from two chained device traversals against dense float64."""
+    import torch
+
+    gx, g, og = env
+    X = og.dense_X().astype(np.float64)
+    N = X.shape[0]
+    if standardized:
+        mu = X.sum(axis=0) / N
+        var = mu * (1 - mu)
+        inv = np.where(var > 0, 1 / np.sqrt(np.where(var > 0, var, 1.0)), 0.0)
+        X = (X - mu[None, :]) * inv[None, :]
+    rng = np.random.default_rng(5)
+    for first, cols in ((UP, g.num_samples), (DOWN, g.num_mutations)):
+        V = rng.standard_normal((3, cols))
+        ref = V @ X @ X.T if first == UP else V @ X.T @ X
+        scale = np.abs(V) @ np.abs(X) @ np.abs(X).T if first == UP else np.abs(V) @ np.abs(X).T @ np.abs(X)
+        got = gx.matmul_gram(g, V, first, standardized=standardized)
+        assert np.all(np.abs(got - ref) <= 1e-11 * scale + 1e-300)
+        dev = gx.matmul_gram(g, torch.from_numpy(V).cuda(), first, standardized=standardized)
+        torch.cuda.synchronize()
+        assert np.array_equal(dev.cpu().numpy(), got)
+    Vi = rng.integers(-3, 4, size=(2, g.num_samples)).astype(np.int64)
+    if not standardized:
+        assert np.array_equal(gx.matmul_gram(g, Vi, UP), Vi @ og.dense_X().astype(np.int64) @ og.dense_X().T)
