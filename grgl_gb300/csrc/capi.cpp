@@ -364,6 +364,16 @@ void grgx_host_free(void* p) { host_free(p); }
 
 void grgx_set_timing(int enabled) { set_timing(enabled); }
 
+// Test hook (not part of the public header): uploads with the plan built on the host instead of
+// the device, so the two builders can be compared.
+extern "C" grgx_status grgx_graph_upload_host_plan(grgx_graph* g) {
+    return guarded([&] {
+        GRGX_CHECK(g, GRGX_ERR_API_MISUSE, "null argument");
+        g->host_plan = true;
+        ensure_device_plan(g);
+    });
+}
+
 // Host-only helper for profiling the plan build (not part of the public header).
 double grgx_plan_benchmark(grgx_graph* g) {
     auto p = build_plan(*g->host);

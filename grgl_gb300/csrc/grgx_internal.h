@@ -108,6 +108,21 @@ struct HostPlan {
 
 std::unique_ptr<HostPlan> build_plan(const HostGraph& g);
 
+// Stages of the plan shared by the host builder (build_plan) and the device builder
+// (plan_device.cu), which computes heights, the renumbering, the UP adjacency and the parent
+// counts on the GPU and lays out rows and chunks here.
+void chunk_level(PullCSR& P, const std::vector<int64_t>& off, int64_t rb, int64_t re);
+void finish_csr(PullCSR& P, const std::vector<int64_t>& off);
+void single_level_csr(PullCSR& P, const std::vector<std::pair<uint32_t, uint32_t>>& pairs);
+// level_begin from the node count of each height
+void plan_levels_from_counts(HostPlan& plan, const std::vector<uint64_t>& perHeight);
+// UP rows (every node of height >= 1) and chunks from the row offsets
+void plan_up_layout(HostPlan& plan, std::vector<int64_t> off);
+// DOWN rows, offsets, down_row_of and chunks from each node's parent count (by new id)
+void plan_down_layout(HostPlan& plan, const std::vector<uint64_t>& pdeg);
+// mutation seeds, missingness seeds and XTX init values (needs old2new / new2old)
+void plan_seeds(HostPlan& plan, const HostGraph& g);
+
 // Device-resident copy of a HostPlan (matmul.cu); freed with destroy_device_plan.
 struct DevicePlan;
 void destroy_device_plan(DevicePlan* p);
@@ -135,4 +150,5 @@ struct grgx_graph {
     std::unique_ptr<grgx::GraphCache, grgx::GraphCacheDeleter> graphs;  // destroyed before `dev`
     std::mutex mu;  // guards plan/dev creation
     int has_coals = -1;  // cached: every non-sample node has a coalescence count (-1 = not computed)
+    bool host_plan = false;  // build the plan on the host (plan.cpp) instead of the device
 };

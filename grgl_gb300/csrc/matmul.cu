@@ -221,6 +221,38 @@ size_t io_size(int dtype) {
 uint32_t* build_down_adj_device(const uint32_t* upAdj, const int* upRows, const ChunkDev* upChunks, long long upChunkCount,
                                 long long E, const std::vector<int32_t>& rowOf, const std::vector<int64_t>& downOff);
 
+uint32_t* build_plan_device(const HostGraph& g, const unsigned long long* dOff, const uint32_t* dAdj, uint64_t E,
+                            HostPlan& plan);
+
+namespace {
+// The E-sized passes of the plan on the device (plan_device.cu): uploads the down CSR, builds
+// the plan, returns the device UP adjacency (null: use the host builder).
+uint32_t* device_plan_build(const HostGraph& hg, std::unique_ptr<HostPlan>& out) {
+    const uint64_t n = hg.num_nodes, E = hg.num_edges();
+    void *dOff = nullptr, *dAdj = nullptr;
+    auto freeAll = [&] {
+        if (dOff) cudaFree(dOff);
+        if (dAdj) cudaFree(dAdj);
+    };
+    auto hp = std::make_unique<HostPlan>();
+    uint32_t* up = nullptr;
+    try {
+        GRGX_CUDA(cudaMalloc(&dOff, (n + 1) * sizeof(uint64_t)));
+        GRGX_CUDA(cudaMalloc(&dAdj, (E ? E : 1) * sizeof(uint32_t)));
+        GRGX_CUDA(cudaMemcpy(dOff, hg.down_off.data(), (n + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice));
+        if (E) GRGX_CUDA(cudaMemcpy(dAdj, hg.down_adj.data(), E * sizeof(uint32_t), cudaMemcpyHostToDevice));
+        up = build_plan_device(hg, static_cast<const unsigned long long*>(dOff), static_cast<const uint32_t*>(dAdj), E,
+                               *hp);
+    } catch (...) {
+        freeAll();
+        throw;
+    }
+    freeAll();
+    if (up) out = std::move(hp);
+    return up;
+}
+}  // namespace
+
 DevicePlan* ensure_device_plan(grgx_graph* g) {
     std::lock_guard<std::mutex> lk(g->mu);
     int device = 0;
@@ -231,11 +263,18 @@ DevicePlan* ensure_device_plan(grgx_graph* g) {
         return g->dev.get();
     }
     setup_pool_once(device);
+    uint32_t* upAdjDev = nullptr;
+    if (!g->plan && !g->host_plan && g->host->num_nodes > 0) upAdjDev = device_plan_build(*g->host, g->plan);
     if (!g->plan) g->plan = build_plan(*g->host);
     const HostPlan& hp = *g->plan;
     std::unique_ptr<DevicePlan, DevicePlanDeleter> d(new DevicePlan());
     d->device = device;
+    if (upAdjDev) {
+        d->allocs.push_back(upAdjDev);
+        d->bytes += static_cast<uint64_t>(hp.up.off.empty() ? 0 : hp.up.off.back()) * sizeof(uint32_t);
+    }
     d->up = upload_csr(*d, hp.up);
+    if (upAdjDev) d->up.adj = upAdjDev;
     d->down = upload_csr(*d, hp.down);
     d->down.adj = build_down_adj_device(d->up.adj, d->up.rows, d->up.chunks,
                                         static_cast<long long>(hp.up.chunks.size()) - 1, hp.down.num_edges,

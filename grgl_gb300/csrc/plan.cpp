@@ -46,6 +46,8 @@ void parallel_for(uint64_t n, const std::function<void(uint64_t, uint64_t, int)>
     for (auto& th : pool) th.join();
 }
 
+}  // namespace
+
 // Chunk target: enough chunks per level to give every SM several waves of warps, never
 // fewer than 64 edges per chunk.
 constexpr int64_t kTargetChunks = 152 * 16 * 8;
@@ -114,8 +116,6 @@ void single_level_csr(PullCSR& P, const std::vector<std::pair<uint32_t, uint32_t
     finish_csr(P, off);
 }
 
-}  // namespace
-
 namespace {
 struct PhaseTimer {
     const char* name;
@@ -129,6 +129,108 @@ struct PhaseTimer {
     }
 };
 }  // namespace
+
+// ---- stages shared by the host and the device builders --------------------------------------
+
+void plan_levels_from_counts(HostPlan& plan, const std::vector<uint64_t>& perHeight) {
+    const uint64_t L = perHeight.size();
+    plan.num_levels = L;
+    plan.level_begin.assign(L + 1, 0);
+    for (uint64_t h = 0; h < L; h++) plan.level_begin[h + 1] = plan.level_begin[h] + perHeight[h];
+}
+
+void plan_up_layout(HostPlan& plan, std::vector<int64_t> off) {
+    PullCSR& P = plan.up;
+    const uint64_t L = plan.num_levels;
+    const uint64_t n = plan.level_begin.empty() ? 0 : plan.level_begin[L];
+    const uint64_t r0 = L > 1 ? plan.level_begin[1] : n;
+    const uint64_t R = n - r0;
+    P.rows.resize(R);
+    for (uint64_t i = 0; i < R; i++) P.rows[i] = static_cast<int32_t>(r0 + i);
+    for (uint64_t h = 1; h < L; h++)
+        chunk_level(P, off, static_cast<int64_t>(plan.level_begin[h] - r0),
+                    static_cast<int64_t>(plan.level_begin[h + 1] - r0));
+    finish_csr(P, off);
+    P.off = std::move(off);
+}
+
+void plan_down_layout(HostPlan& plan, const std::vector<uint64_t>& pdeg) {
+    PullCSR& P = plan.down;
+    const uint64_t L = plan.num_levels;
+    const uint64_t n = pdeg.size();
+    // Row order: heights descending, ids ascending inside a height.
+    std::vector<uint32_t> rowNode;
+    rowNode.reserve(n);
+    for (uint64_t hh = L; hh > 0; hh--) {
+        const uint64_t h = hh - 1;
+        for (uint64_t id = plan.level_begin[h]; id < plan.level_begin[h + 1]; id++)
+            if (pdeg[id]) rowNode.push_back(static_cast<uint32_t>(id));
+    }
+    const uint64_t R = rowNode.size();
+    std::vector<int64_t> off(R + 1, 0);
+    for (uint64_t i = 0; i < R; i++) off[i + 1] = off[i] + static_cast<int64_t>(pdeg[rowNode[i]]);
+    P.rows.assign(rowNode.begin(), rowNode.end());
+    plan.down_row_of.assign(n, -1);
+    for (uint64_t i = 0; i < R; i++) plan.down_row_of[rowNode[i]] = static_cast<int32_t>(i);
+    // Level ranges over rows.
+    uint64_t rb = 0;
+    for (uint64_t hh = L; hh > 0; hh--) {
+        const uint64_t h = hh - 1;
+        uint64_t re = rb;
+        while (re < R && rowNode[re] >= plan.level_begin[h] && rowNode[re] < plan.level_begin[h + 1]) re++;
+        chunk_level(P, off, static_cast<int64_t>(rb), static_cast<int64_t>(re));
+        rb = re;
+    }
+    finish_csr(P, off);
+    P.off = std::move(off);
+}
+
+void plan_seeds(HostPlan& plan, const HostGraph& g) {
+    const uint64_t n = g.num_nodes, N = g.num_samples;
+    const auto& o2n = plan.old2new;
+    const auto& n2o = plan.new2old;
+    plan.mut_new.assign(g.num_mutations, INVALID_NODE);
+    std::vector<std::pair<uint32_t, uint32_t>> pairs;
+    for (uint64_t m = 0; m < g.num_mutations; m++) {
+        if (g.mut_node[m] != INVALID_NODE) {
+            plan.mut_new[m] = o2n[g.mut_node[m]];
+            pairs.emplace_back(plan.mut_new[m], static_cast<uint32_t>(m));
+        }
+    }
+    std::sort(pairs.begin(), pairs.end());
+    single_level_csr(plan.seed, pairs);
+    plan.has_miss = !g.miss_node.empty();
+    plan.miss_new.assign(g.num_mutations, INVALID_NODE);
+    pairs.clear();
+    if (plan.has_miss) {
+        for (uint64_t m = 0; m < g.num_mutations; m++) {
+            if (g.miss_node[m] != INVALID_NODE) {
+                plan.miss_new[m] = o2n[g.miss_node[m]];
+                pairs.emplace_back(plan.miss_new[m], static_cast<uint32_t>(m));
+            }
+        }
+        std::sort(pairs.begin(), pairs.end());
+    }
+    single_level_csr(plan.miss, pairs);
+
+    // xtx init values by new id
+    plan.xtx_new.assign(n, 0);
+    plan.has_coals = true;
+    for (uint64_t id = 0; id < n; id++) {
+        const uint32_t old = n2o[id];
+        uint32_t c = 0;
+        if (old >= N) {
+            const uint64_t idx = old - N;
+            c = (idx < g.coals.size()) ? g.coals[idx] : COAL_NOT_SET;
+        }
+        if (c == COAL_NOT_SET) {
+            plan.has_coals = false;
+            plan.xtx_new[id] = COAL_NOT_SET;
+        } else {
+            plan.xtx_new[id] = c * 2u;
+        }
+    }
+}
 
 std::unique_ptr<HostPlan> build_plan(const HostGraph& g) {
     PhaseTimer timer{"plan"};
@@ -184,12 +286,11 @@ std::unique_ptr<HostPlan> build_plan(const HostGraph& g) {
     uint32_t maxH = 0;
     for (uint64_t v = 0; v < n; v++) maxH = std::max(maxH, height[v]);
     const uint64_t L = (n == 0) ? 0 : maxH + 1;
-    plan->num_levels = L;
 
     // ---- renumbering (stable counting sort by height) ---------------------------------------
-    plan->level_begin.assign(L + 1, 0);
-    for (uint64_t v = 0; v < n; v++) plan->level_begin[height[v] + 1]++;
-    for (uint64_t h = 0; h < L; h++) plan->level_begin[h + 1] += plan->level_begin[h];
+    std::vector<uint64_t> perHeight(L, 0);
+    for (uint64_t v = 0; v < n; v++) perHeight[height[v]]++;
+    plan_levels_from_counts(*plan, perHeight);
     plan->old2new.resize(n);
     plan->new2old.resize(n);
     {
@@ -209,11 +310,9 @@ std::unique_ptr<HostPlan> build_plan(const HostGraph& g) {
         PullCSR& P = plan->up;
         const uint64_t r0 = L > 1 ? plan->level_begin[1] : n;
         const uint64_t R = n - r0;
-        P.rows.resize(R);
         std::vector<int64_t> off(R + 1, 0);
         for (uint64_t i = 0; i < R; i++) {
             const uint32_t old = n2o[r0 + i];
-            P.rows[i] = static_cast<int32_t>(r0 + i);
             off[i + 1] = off[i] + static_cast<int64_t>(g.down_off[old + 1] - g.down_off[old]);
         }
         P.adj.resize(off[R]);
@@ -225,11 +324,7 @@ std::unique_ptr<HostPlan> build_plan(const HostGraph& g) {
                     P.adj[w++] = o2n[g.down_adj[x]] | (x == g.down_off[old] ? HEAD_BIT : 0u);
             }
         });
-        for (uint64_t h = 1; h < L; h++)
-            chunk_level(P, off, static_cast<int64_t>(plan->level_begin[h] - r0),
-                        static_cast<int64_t>(plan->level_begin[h + 1] - r0));
-        finish_csr(P, off);
-        P.off = std::move(off);
+        plan_up_layout(*plan, std::move(off));
     }
 
     timer.lap("up csr");
@@ -237,7 +332,6 @@ std::unique_ptr<HostPlan> build_plan(const HostGraph& g) {
     // The host counts parents per node (parallel, per-thread counters) to lay out rows, offsets
     // and chunks; the adjacency itself is built on the device from the UP CSR (plan_gpu.cu).
     {
-        PullCSR& P = plan->down;
         const int T = (g.num_edges() < (1u << 20)) ? 1 : host_threads();
         // parent ranges balanced by edge count
         std::vector<uint64_t> pb(T + 1, 0);
@@ -251,7 +345,6 @@ std::unique_ptr<HostPlan> build_plan(const HostGraph& g) {
                 pb[t] = static_cast<uint64_t>(std::lower_bound(cum.begin(), cum.end(), cum[n] * t / T) - cum.begin());
             pb[T] = n;
         }
-        timer.lap("down.ranges");
         std::vector<std::vector<uint32_t>> cnt(T, std::vector<uint32_t>(n, 0));
         parallel_for(T, [&](uint64_t b, uint64_t e, int) {
             for (uint64_t t = b; t < e; t++) {
@@ -271,77 +364,11 @@ std::unique_ptr<HostPlan> build_plan(const HostGraph& g) {
                 pdeg[c] = d;
             }
         });
-        // Row order: heights descending, ids ascending inside a height.
-        std::vector<uint32_t> rowNode;
-        rowNode.reserve(n);
-        for (uint64_t hh = L; hh > 0; hh--) {
-            const uint64_t h = hh - 1;
-            for (uint64_t id = plan->level_begin[h]; id < plan->level_begin[h + 1]; id++)
-                if (pdeg[id]) rowNode.push_back(static_cast<uint32_t>(id));
-        }
-        const uint64_t R = rowNode.size();
-        std::vector<int64_t> off(R + 1, 0);
-        for (uint64_t i = 0; i < R; i++) off[i + 1] = off[i] + static_cast<int64_t>(pdeg[rowNode[i]]);
-        P.rows.assign(rowNode.begin(), rowNode.end());
-        plan->down_row_of.assign(n, -1);
-        for (uint64_t i = 0; i < R; i++) plan->down_row_of[rowNode[i]] = static_cast<int32_t>(i);
-        timer.lap("down.rows");
-        // Level ranges over rows.
-        uint64_t rb = 0;
-        for (uint64_t hh = L; hh > 0; hh--) {
-            const uint64_t h = hh - 1;
-            uint64_t re = rb;
-            while (re < R && rowNode[re] >= plan->level_begin[h] && rowNode[re] < plan->level_begin[h + 1]) re++;
-            chunk_level(P, off, static_cast<int64_t>(rb), static_cast<int64_t>(re));
-            rb = re;
-        }
-        finish_csr(P, off);
-        P.off = std::move(off);
+        plan_down_layout(*plan, pdeg);
     }
 
     timer.lap("down csr");
-    // ---- mutation seeds / gathers -----------------------------------------------------------
-    plan->mut_new.assign(g.num_mutations, INVALID_NODE);
-    std::vector<std::pair<uint32_t, uint32_t>> pairs;
-    for (uint64_t m = 0; m < g.num_mutations; m++) {
-        if (g.mut_node[m] != INVALID_NODE) {
-            plan->mut_new[m] = o2n[g.mut_node[m]];
-            pairs.emplace_back(plan->mut_new[m], static_cast<uint32_t>(m));
-        }
-    }
-    std::sort(pairs.begin(), pairs.end());
-    single_level_csr(plan->seed, pairs);
-    plan->has_miss = !g.miss_node.empty();
-    plan->miss_new.assign(g.num_mutations, INVALID_NODE);
-    pairs.clear();
-    if (plan->has_miss) {
-        for (uint64_t m = 0; m < g.num_mutations; m++) {
-            if (g.miss_node[m] != INVALID_NODE) {
-                plan->miss_new[m] = o2n[g.miss_node[m]];
-                pairs.emplace_back(plan->miss_new[m], static_cast<uint32_t>(m));
-            }
-        }
-        std::sort(pairs.begin(), pairs.end());
-    }
-    single_level_csr(plan->miss, pairs);
-
-    // ---- xtx init values by new id ------------------------------------------------------------
-    plan->xtx_new.assign(n, 0);
-    plan->has_coals = true;
-    for (uint64_t id = 0; id < n; id++) {
-        const uint32_t old = n2o[id];
-        uint32_t c = 0;
-        if (old >= N) {
-            const uint64_t idx = old - N;
-            c = (idx < g.coals.size()) ? g.coals[idx] : COAL_NOT_SET;
-        }
-        if (c == COAL_NOT_SET) {
-            plan->has_coals = false;
-            plan->xtx_new[id] = COAL_NOT_SET;
-        } else {
-            plan->xtx_new[id] = c * 2u;
-        }
-    }
+    plan_seeds(*plan, g);
     timer.lap("seeds/xtx");
     return plan;
 }
