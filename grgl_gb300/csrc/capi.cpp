@@ -148,7 +148,7 @@ grgx_status grgx_graph_generate(uint64_t num_samples, uint64_t num_mutations, ui
 grgx_status grgx_graph_subset(const grgx_graph* g, const uint32_t* mutation_ids, uint64_t n, grgx_graph** out) {
     return guarded([&] {
         GRGX_CHECK(g && out && (n == 0 || mutation_ids), GRGX_ERR_API_MISUSE, "null argument");
-        const HostGraph& h = *g->host;
+        const HostGraph& h = const_cast<grgx_graph*>(g)->host_edges();
         std::vector<uint8_t> keep(h.num_nodes, 0);
         for (uint64_t s = 0; s < h.num_samples; s++) keep[s] = 1;
         std::vector<uint32_t> stack;
@@ -228,7 +228,8 @@ grgx_status grgx_graph_info_get(const grgx_graph* g, grgx_graph_info* out) {
         out->num_samples = h.num_samples;
         out->num_mutations = h.num_mutations;
         out->ploidy = h.ploidy;
-        out->num_levels = g->dev ? device_plan_levels(g) : count_levels(h);
+        // an encoded graph's levels are known once its plan is built
+        out->num_levels = g->dev ? device_plan_levels(g) : (h.encoded() ? 0 : count_levels(h));
         out->has_missing = h.miss_node.empty() ? 0 : 1;
         bool coals = h.coals.size() >= h.num_nodes - h.num_samples;
         for (uint64_t i = 0; coals && i < h.num_nodes - h.num_samples; i++) coals = (h.coals[i] != COAL_NOT_SET);
@@ -241,7 +242,7 @@ grgx_status grgx_graph_export(const grgx_graph* g, uint64_t* down_off, uint32_t*
                               uint32_t* miss_node, uint32_t* coals) {
     return guarded([&] {
         GRGX_CHECK(g, GRGX_ERR_API_MISUSE, "null argument");
-        const HostGraph& h = *g->host;
+        const HostGraph& h = (down_off || down_adj) ? const_cast<grgx_graph*>(g)->host_edges() : *g->host;
         if (down_off) std::memcpy(down_off, h.down_off.data(), h.down_off.size() * sizeof(uint64_t));
         if (down_adj && !h.down_adj.empty())
             std::memcpy(down_adj, h.down_adj.data(), h.down_adj.size() * sizeof(uint32_t));
@@ -376,7 +377,7 @@ extern "C" grgx_status grgx_graph_upload_host_plan(grgx_graph* g) {
 
 // Host-only helper for profiling the plan build (not part of the public header).
 double grgx_plan_benchmark(grgx_graph* g) {
-    auto p = build_plan(*g->host);
+    auto p = build_plan(g->host_edges());
     return static_cast<double>(p->up.adj.size());
 }
 

@@ -1,4 +1,6 @@
-// .grg file reader: the subset of GRGL's immutable load that the matmul path needs.
+// .grg file reader: the subset of GRGL's immutable load that the matmul path needs.  The edge
+// buckets stay encoded (as the reference's CSR storage keeps them, csr_storage.h:407-429)
+// until the device plan decodes them on the GPU or a host consumer materialises them.
 //
 // Layout read here (src/serialize.cpp:815-890 readImmutableGrg, :697-758 readGrgCommon,
 // include/grgl/common.h:181-202 header):
@@ -128,29 +130,12 @@ std::unique_ptr<HostGraph> load_grg_file(const std::string& path) {
     } else {
         nodeIdx = r.array<uint64_t>(h.nodeCount + 1);
     }
-    g->down_off.assign(h.nodeCount + 1, 0);
-    g->down_adj.reserve(h.edgeCount);
-    const uint8_t* base = buckets.data();
-    const uint8_t* end = base + buckets.size();
-    for (uint64_t v = 0; v < h.nodeCount; v++) {
-        const uint64_t b0 = nodeIdx[v], b1 = nodeIdx[v + 1];
-        if (b0 < b1) {
-            GRGX_CHECK(b1 <= edgeBytes, GRGX_ERR_BAD_FILE, "Malformed GRG file");
-            const uint8_t* p = base + b0;
-            uint32_t count = 0;
-            p += decode_varint(p, end, &count);
-            uint32_t prev = 0;
-            for (uint32_t i = 0; i < count; i++) {
-                uint32_t delta = 0;
-                p += decode_varint(p, end, &delta);
-                prev += delta;
-                GRGX_CHECK(prev < h.nodeCount, GRGX_ERR_BAD_FILE, "Malformed GRG file");
-                g->down_adj.push_back(prev);
-            }
-        }
-        g->down_off[v + 1] = g->down_adj.size();
-    }
-    GRGX_CHECK(g->down_adj.size() == h.edgeCount, GRGX_ERR_BAD_FILE, "Malformed GRG file");
+    for (uint64_t v = 0; v < h.nodeCount; v++)
+        GRGX_CHECK(nodeIdx[v] <= nodeIdx[v + 1] && nodeIdx[v + 1] <= edgeBytes, GRGX_ERR_BAD_FILE,
+                   "Malformed GRG file");
+    g->enc_buckets = std::move(buckets);
+    g->enc_index = std::move(nodeIdx);
+    g->enc_edges = h.edgeCount;
 
     g->mut_node = r.array<uint32_t>(h.mutationCount);
     for (uint32_t& n : g->mut_node)
@@ -184,6 +169,39 @@ std::unique_ptr<HostGraph> load_grg_file(const std::string& path) {
             GRGX_CHECK(n == INVALID_NODE || n < h.nodeCount, GRGX_ERR_BAD_FILE, "Malformed GRG file");
     }
     return g;
+}
+
+void materialize_edges(HostGraph& g) {
+    if (!g.encoded()) return;
+    const uint64_t n = g.num_nodes;
+    std::vector<uint64_t> off(n + 1, 0);
+    std::vector<uint32_t> adj;
+    adj.reserve(g.enc_edges);
+    const uint8_t* base = g.enc_buckets.data();
+    const uint8_t* end = base + g.enc_buckets.size();
+    for (uint64_t v = 0; v < n; v++) {
+        const uint64_t b0 = g.enc_index[v], b1 = g.enc_index[v + 1];
+        if (b0 < b1) {
+            const uint8_t* p = base + b0;
+            uint32_t count = 0;
+            p += decode_varint(p, end, &count);
+            uint32_t prev = 0;
+            for (uint32_t i = 0; i < count; i++) {
+                uint32_t delta = 0;
+                p += decode_varint(p, end, &delta);
+                prev += delta;
+                GRGX_CHECK(prev < n, GRGX_ERR_BAD_FILE, "Malformed GRG file");
+                adj.push_back(prev);
+            }
+        }
+        off[v + 1] = adj.size();
+    }
+    GRGX_CHECK(adj.size() == g.enc_edges, GRGX_ERR_BAD_FILE, "Malformed GRG file");
+    g.down_off = std::move(off);
+    g.down_adj = std::move(adj);
+    std::vector<uint8_t>().swap(g.enc_buckets);
+    std::vector<uint64_t>().swap(g.enc_index);
+    g.enc_edges = 0;
 }
 
 }  // namespace grgx

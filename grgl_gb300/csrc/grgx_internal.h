@@ -45,8 +45,19 @@ struct HostGraph {
     std::vector<uint32_t> miss_node;  // empty, or num_mutations (INVALID_NODE when none)
     std::vector<uint32_t> coals;      // empty, or num_nodes - num_samples
     std::vector<uint64_t> mut_pos;    // optional positions (bp)
-    uint64_t num_edges() const { return down_adj.size(); }
+    // A graph read from a .grg file keeps its edges as the file stores them -- one vbyte
+    // bucket per node -- until something needs them: the device plan decodes the buckets on
+    // the GPU (grg_decode.cu); host consumers call materialize_edges first.
+    std::vector<uint8_t> enc_buckets;
+    std::vector<uint64_t> enc_index;  // bucket byte offset of each node, num_nodes + 1
+    uint64_t enc_edges = 0;           // edge count from the file header
+    bool encoded() const { return !enc_index.empty(); }
+    uint64_t num_edges() const { return encoded() ? enc_edges : down_adj.size(); }
 };
+
+// Decodes the vbyte buckets of an encoded graph into down_off / down_adj on the host and drops
+// the encoded copy (no-op for a decoded graph).  Throws GRGX_ERR_BAD_FILE on malformed buckets.
+void materialize_edges(HostGraph& g);
 
 // Load a .grg file (format 5.x, serialize.cpp:815-890 + readGrgCommon :697-758).
 std::unique_ptr<HostGraph> load_grg_file(const std::string& path);
@@ -144,6 +155,12 @@ void set_last_error(const std::string& msg);
 
 // The opaque handle behind grgx_graph*.
 struct grgx_graph {
+    // The host graph with its edges decoded (decodes an encoded graph once).
+    grgx::HostGraph& host_edges() {
+        std::lock_guard<std::mutex> lk(edges_mu);
+        grgx::materialize_edges(*host);
+        return *host;
+    }
     std::unique_ptr<grgx::HostGraph> host;
     std::unique_ptr<grgx::HostPlan> plan;
     std::unique_ptr<grgx::DevicePlan, grgx::DevicePlanDeleter> dev;
@@ -151,4 +168,5 @@ struct grgx_graph {
     std::mutex mu;  // guards plan/dev creation
     int has_coals = -1;  // cached: every non-sample node has a coalescence count (-1 = not computed)
     bool host_plan = false;  // build the plan on the host (plan.cpp) instead of the device
+    std::mutex edges_mu;     // guards materialize_edges of `host`
 };

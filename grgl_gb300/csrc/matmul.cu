@@ -224,9 +224,12 @@ uint32_t* build_down_adj_device(const uint32_t* upAdj, const int* upRows, const 
 uint32_t* build_plan_device(const HostGraph& g, const unsigned long long* dOff, const uint32_t* dAdj, uint64_t E,
                             HostPlan& plan);
 
+void decode_edges_device(const HostGraph& hg, void** dOff, void** dAdj);
+
 namespace {
-// The E-sized passes of the plan on the device (plan_device.cu): uploads the down CSR, builds
-// the plan, returns the device UP adjacency (null: use the host builder).
+// The E-sized passes of the plan on the device (plan_device.cu) from the down CSR, uploaded
+// from the host or decoded on the device from an encoded graph's vbyte buckets; returns the
+// device UP adjacency (null: use the host builder).
 uint32_t* device_plan_build(const HostGraph& hg, std::unique_ptr<HostPlan>& out) {
     const uint64_t n = hg.num_nodes, E = hg.num_edges();
     void *dOff = nullptr, *dAdj = nullptr;
@@ -237,10 +240,14 @@ uint32_t* device_plan_build(const HostGraph& hg, std::unique_ptr<HostPlan>& out)
     auto hp = std::make_unique<HostPlan>();
     uint32_t* up = nullptr;
     try {
-        GRGX_CUDA(cudaMalloc(&dOff, (n + 1) * sizeof(uint64_t)));
-        GRGX_CUDA(cudaMalloc(&dAdj, (E ? E : 1) * sizeof(uint32_t)));
-        GRGX_CUDA(cudaMemcpy(dOff, hg.down_off.data(), (n + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice));
-        if (E) GRGX_CUDA(cudaMemcpy(dAdj, hg.down_adj.data(), E * sizeof(uint32_t), cudaMemcpyHostToDevice));
+        if (hg.encoded()) {
+            decode_edges_device(hg, &dOff, &dAdj);
+        } else {
+            GRGX_CUDA(cudaMalloc(&dOff, (n + 1) * sizeof(uint64_t)));
+            GRGX_CUDA(cudaMalloc(&dAdj, (E ? E : 1) * sizeof(uint32_t)));
+            GRGX_CUDA(cudaMemcpy(dOff, hg.down_off.data(), (n + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice));
+            if (E) GRGX_CUDA(cudaMemcpy(dAdj, hg.down_adj.data(), E * sizeof(uint32_t), cudaMemcpyHostToDevice));
+        }
         up = build_plan_device(hg, static_cast<const unsigned long long*>(dOff), static_cast<const uint32_t*>(dAdj), E,
                                *hp);
     } catch (...) {
@@ -265,7 +272,7 @@ DevicePlan* ensure_device_plan(grgx_graph* g) {
     setup_pool_once(device);
     uint32_t* upAdjDev = nullptr;
     if (!g->plan && !g->host_plan && g->host->num_nodes > 0) upAdjDev = device_plan_build(*g->host, g->plan);
-    if (!g->plan) g->plan = build_plan(*g->host);
+    if (!g->plan) g->plan = build_plan(g->host_edges());
     const HostPlan& hp = *g->plan;
     std::unique_ptr<DevicePlan, DevicePlanDeleter> d(new DevicePlan());
     d->device = device;

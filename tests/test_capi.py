@@ -155,3 +155,19 @@ def test_window_tree_equals_reference_construction(gx):
     for direction, cols in ((UP, 1000), (DOWN, 10000)):
         V = rng.integers(-1000, 1000, size=(2, cols)).astype(np.int64)
         assert np.array_equal(oracle.matmul(og, V, direction), oracle.matmul(ref, V, direction))
+
+
+def test_loader_keeps_buckets_encoded_until_needed(gx, tmp_path):
+    """A loaded graph reports its sizes from the header; a corrupt bucket surfaces, with the
+    loader's message, when the edges are first decoded (here on the host, by an export)."""
+    raw = bytearray((GOLDEN / "t200.grg").read_bytes())
+    g = gx.load_immutable_grg(str(GOLDEN / "t200.grg"))
+    o = oracle.read_grg(GOLDEN / "t200.grg")
+    assert g.num_edges == o.num_edges and g.num_nodes == o.num_nodes
+    raw[136:142] = b"\xff" * 6  # the first bucket's count: a varint longer than five bytes
+    bad = tmp_path / "badbucket.grg"
+    bad.write_bytes(bytes(raw))
+    gb = gx.load_immutable_grg(str(bad))
+    assert gb is not None and gb.num_edges == o.num_edges
+    with pytest.raises(RuntimeError, match="Malformed GRG file"):
+        gb.export_arrays()
