@@ -203,11 +203,7 @@ __device__ __forceinline__ void sweep_chunk(const SweepParams<typename Op::S>& p
             }
             if (anyHead == 0u) {
                 // no row starts in this step: every edge continues the current row
-#pragma unroll
-                for (int u = 0; u < BATCH; u++) {
-                    acc.add(v[u]);
-                    if (kChains && (u & 3) == 3) acc.settle();
-                }
+                acc.template add_block<BATCH>(v);
                 continue;
             }
 #pragma unroll

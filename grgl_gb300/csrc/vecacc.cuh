@@ -40,6 +40,11 @@ template <class Op, int VW> struct VecAcc {
 #pragma unroll
         for (int i = 0; i < VW; i++) Op::add(a[i], v[i]);
     }
+    // N consecutive edges of one row (the sweep's boundary-free steps).
+    template <int N> __device__ __forceinline__ void add_block(const S (*v)[VW]) {
+#pragma unroll
+        for (int u = 0; u < N; u++) add(v[u]);
+    }
     __device__ __forceinline__ void merge(const VecAcc& o) {
 #pragma unroll
         for (int i = 0; i < VW; i++) Op::merge(a[i], o.a[i]);
@@ -67,6 +72,13 @@ template <> struct VecAcc<AddF64S, 1> {
     F64Run a[1];
     __device__ __forceinline__ void zero() { a[0] = AddF64S::zero(); }
     __device__ __forceinline__ void add(const DF* v) { AddF64S::add(a[0], v[0]); }
+    template <int N> __device__ __forceinline__ void add_block(const DF (*v)[1]) {
+#pragma unroll
+        for (int u = 0; u < N; u++) {
+            add(v[u]);
+            if ((u & 3) == 3) settle();
+        }
+    }
     __device__ __forceinline__ void merge(const VecAcc& o) { AddF64S::merge(a[0], o.a[0]); }
     __device__ __forceinline__ VecAcc shfl_xor(int m) const { return {{AddF64S::shfl_xor(a[0], m)}}; }
     __device__ __forceinline__ VecAcc shfl_up(int d) const { return {{AddF64S::shfl_up(a[0], d)}}; }
@@ -76,6 +88,13 @@ template <> struct VecAcc<AddF64S, 1> {
     __device__ __forceinline__ void flush() { AddF64S::flush(a[0]); }
 };
 
+// In boundary-free steps the edges of a row are added in plain float32 four at a time, as a
+// two-level tree, before one TwoSum takes the quad into the compensated (hi, lo) pair.  A node's
+// error then stays within 2u * sum|x| (the tree roundings) + u * |value| (its final rounding),
+// u = 2^-24, for a quarter of the TwoSums of one per edge; steps with a row boundary keep one
+// TwoSum per edge.
+constexpr int kF32PreSum = 4;
+
 // Compensated float32, columns in pairs.
 template <int NP> struct PackedF32C {
     float2 hi[NP], lo[NP];
@@ -83,13 +102,33 @@ template <int NP> struct PackedF32C {
 #pragma unroll
         for (int j = 0; j < NP; j++) hi[j] = lo[j] = make_float2(0.0f, 0.0f);
     }
+    __device__ __forceinline__ void add_pair2(int j, float2 x) {
+        float2 s, e;
+        two_sum2(hi[j], x, s, e);
+        lo[j] = add2(lo[j], e);
+        hi[j] = s;
+    }
     __device__ __forceinline__ void add(const float* v) {
 #pragma unroll
-        for (int j = 0; j < NP; j++) {
-            float2 s, e;
-            two_sum2(hi[j], make_float2(v[2 * j], v[2 * j + 1]), s, e);
-            lo[j] = add2(lo[j], e);
-            hi[j] = s;
+        for (int j = 0; j < NP; j++) add_pair2(j, make_float2(v[2 * j], v[2 * j + 1]));
+    }
+    template <int N> __device__ __forceinline__ void add_block(const float (*v)[2 * NP]) {
+        static_assert(N % kF32PreSum == 0, "block of whole pre-sums");
+#pragma unroll
+        for (int u = 0; u < N; u += kF32PreSum) {
+#pragma unroll
+            for (int j = 0; j < NP; j++) {
+                float2 t = make_float2(v[u][2 * j], v[u][2 * j + 1]);
+                if (kF32PreSum == 2) {
+                    t = add2(t, make_float2(v[u + 1][2 * j], v[u + 1][2 * j + 1]));
+                } else if (kF32PreSum == 4) {
+                    const float2 b = make_float2(v[u + 1][2 * j], v[u + 1][2 * j + 1]);
+                    const float2 c = make_float2(v[u + 2][2 * j], v[u + 2][2 * j + 1]);
+                    const float2 d = make_float2(v[u + 3][2 * j], v[u + 3][2 * j + 1]);
+                    t = add2(add2(t, b), add2(c, d));
+                }
+                add_pair2(j, t);
+            }
         }
     }
     __device__ __forceinline__ void merge(const PackedF32C& o) {
@@ -158,6 +197,13 @@ template <int NP> struct PackedF64S {
             lo[j] = add2(lo[j], add2(e, xl));
             hi[j] = s;
             p[j] = add2(p[j], xh);
+        }
+    }
+    template <int N> __device__ __forceinline__ void add_block(const DF (*v)[2 * NP]) {
+#pragma unroll
+        for (int u = 0; u < N; u++) {
+            add(v[u]);
+            if ((u & 3) == 3) settle();
         }
     }
     __device__ __forceinline__ void settle() {
