@@ -46,9 +46,11 @@ __global__ void rowmax_kernel(const double* __restrict__ src, long long K, long 
              c += (long long)gridDim.x * blockDim.x) {
             const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(src[k * ld + c])) &
                                          0x7fffffffffffffffull;
-            if ((b & kExpMask) != kExpMask) {  // finite only
+            if ((b & kExpMask) != kExpMask) {  // finite
                 m = b > m ? b : m;
                 if (b != 0) mn = b < mn ? b : mn;
+            } else {
+                mn = 0;  // inf or nan: marks the row for the FP64 path
             }
         }
         for (int o = 16; o > 0; o >>= 1) {
@@ -69,7 +71,7 @@ __global__ void rowmax_kernel(const double* __restrict__ src, long long K, long 
                 q = redMin[w] < q ? redMin[w] : q;
             }
             if (r) atomicMax(rowmax + k, r);
-            if (q != ~0ull) atomicMin(rowmin + k, q);
+            if (q != ~0ull) atomicMin(rowmin + k, q);  // 0 when the row holds an inf or a nan
         }
         __syncthreads();
     }
@@ -82,6 +84,10 @@ __global__ void decide_kernel(const unsigned long long* __restrict__ rowmax, con
     __syncthreads();
     for (long long k = threadIdx.x; k < K; k += blockDim.x) {
         const unsigned long long mx = rowmax[k], mn = rowmin[k];
+        if (mn == 0) {  // an inf or a nan: only the FP64 path carries IEEE semantics through
+            wide = 1;
+            continue;
+        }
         if (mx == 0 || mn == ~0ull) continue;
         const int emax = static_cast<int>((mx >> 52) & 0x7ff), emin = static_cast<int>((mn >> 52) & 0x7ff);
         const int re = row_exp(rowmax, k);

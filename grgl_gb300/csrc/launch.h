@@ -62,8 +62,8 @@ void launch_fill_u64(unsigned long long* p, long long n, unsigned long long v, c
 // Also folds the smallest nonzero finite magnitude into rowmin[k] (filled with ~0 first).
 void launch_rowmax(const double* src, long long K, long long ld, long long cols, unsigned long long* rowmax,
                    unsigned long long* rowmin, cudaStream_t s);
-// gate[0] = 1 when some row spans more binades than the float-pair path holds (the call then
-// runs on the FP64 pipe), else 0.
+// gate[0] = 1 when some row spans more binades than the float-pair path holds, or holds an inf
+// or a nan (the call then runs on the FP64 pipe), else 0.
 void launch_decide_f64_path(const unsigned long long* rowmax, const unsigned long long* rowmin, long long K, int* gate,
                             cudaStream_t s);
 void launch_load_rows_df(const double* src, long long K, long long ld, long long R, int mode, long long div,

@@ -100,7 +100,9 @@ Layout choose_layout(int dtype, long long K, bool plainF32, bool nativeF64) {
     case GRGX_BOOL: L.kind = Kind::XOR; L.ssize = 4; base = (K + 31) / 32; break;
     default: L.kind = Kind::U32; L.ssize = 4; break;
     }
-    L.asize = (L.kind == Kind::F32C) ? 8 : (L.kind == Kind::F64S ? 24 : L.ssize);
+    L.asize = (L.kind == Kind::F32C || L.kind == Kind::F64S) ? static_cast<int>(L.kind == Kind::F32C ? sizeof(F32Pair)
+                                                                                               : sizeof(F64Run))
+                                                              : L.ssize;
     const int maxVw = 16 / L.ssize;
     if (base == 1) {
         L.stride = 1; L.vw = 1; L.g = 1; L.ntiles = 1;

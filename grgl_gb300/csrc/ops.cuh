@@ -135,21 +135,21 @@ struct AddF32C {
 // renormalised (FastTwoSum), and every 32 additions the run is folded into a double.  A run's
 // error is then a few u^2 (u = 2^-24) per renormalised period -- ~8 * (16 + 1) u^2 sum|x| ~ 5e-13
 // of the terms' magnitudes over 32 additions -- and the double chain adds 1.1e-16 per fold.
-// `p` keeps the plain float sum of the high parts, which carries IEEE inf/nan through exactly
-// when an input is not finite.
+// Rows holding an inf or a nan never reach this path: the device-side gate sends such calls to
+// native FP64 (io_df.cu), so every value here is finite and far from float overflow.
 struct alignas(8) DF {
     float hi, lo;
 };
 
 struct F64Run {
     double acc;
-    float hi, lo, p, pad;
+    float hi, lo;
 };
 
 struct AddF64S {
     using S = DF;
     using A = F64Run;
-    static __device__ __forceinline__ A zero() { return {0.0, 0.0f, 0.0f, 0.0f, 0.0f}; }
+    static __device__ __forceinline__ A zero() { return {0.0, 0.0f, 0.0f}; }
     // normalised float-float addition (merges of partial sums)
     static __device__ __forceinline__ void run_add(float& hi, float& lo, float xh, float xl) {
         const float s = __fadd_rn(hi, xh);
@@ -166,7 +166,6 @@ struct AddF64S {
         const float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(x.hi, bb));
         a.lo = __fadd_rn(a.lo, __fadd_rn(e, x.lo));
         a.hi = s;
-        a.p = __fadd_rn(a.p, x.hi);
     }
     static __device__ __forceinline__ void settle(A& a) {
         const float h = __fadd_rn(a.hi, a.lo);
@@ -174,24 +173,21 @@ struct AddF64S {
         a.hi = h;
     }
     static __device__ __forceinline__ double run_value(const A& a) {
-        return isfinite(a.p) ? (static_cast<double>(a.hi) + static_cast<double>(a.lo)) : static_cast<double>(a.p);
+        return static_cast<double>(a.hi) + static_cast<double>(a.lo);
     }
     static __device__ __forceinline__ void flush(A& a) {
         a.acc += run_value(a);
-        a.hi = a.lo = a.p = 0.0f;
+        a.hi = a.lo = 0.0f;
     }
     static __device__ __forceinline__ void merge(A& a, const A& b) {
         a.acc += b.acc;
         run_add(a.hi, a.lo, b.hi, b.lo);
-        a.p = __fadd_rn(a.p, b.p);
     }
     static __device__ __forceinline__ A shfl_xor(const A& a, int m) {
         A r;
         r.acc = __shfl_xor_sync(FULL_MASK, a.acc, m);
         r.hi = __shfl_xor_sync(FULL_MASK, a.hi, m);
         r.lo = __shfl_xor_sync(FULL_MASK, a.lo, m);
-        r.p = __shfl_xor_sync(FULL_MASK, a.p, m);
-        r.pad = 0.0f;
         return r;
     }
     static __device__ __forceinline__ A shfl_up(const A& a, int d) {
@@ -199,8 +195,6 @@ struct AddF64S {
         r.acc = __shfl_up_sync(FULL_MASK, a.acc, d);
         r.hi = __shfl_up_sync(FULL_MASK, a.hi, d);
         r.lo = __shfl_up_sync(FULL_MASK, a.lo, d);
-        r.p = __shfl_up_sync(FULL_MASK, a.p, d);
-        r.pad = 0.0f;
         return r;
     }
     static __device__ __forceinline__ A shfl_down(const A& a, int d) {
@@ -208,8 +202,6 @@ struct AddF64S {
         r.acc = __shfl_down_sync(FULL_MASK, a.acc, d);
         r.hi = __shfl_down_sync(FULL_MASK, a.hi, d);
         r.lo = __shfl_down_sync(FULL_MASK, a.lo, d);
-        r.p = __shfl_down_sync(FULL_MASK, a.p, d);
-        r.pad = 0.0f;
         return r;
     }
     static __device__ __forceinline__ S split(double v) {

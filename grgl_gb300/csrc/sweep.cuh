@@ -105,11 +105,10 @@ __device__ __forceinline__ unsigned long long ld_cg(const unsigned long long* p)
 __device__ __forceinline__ double ld_cg(const double* p) { return __ldcg(p); }
 __device__ __forceinline__ float ld_cg(const float* p) { return __ldcg(p); }
 __device__ __forceinline__ F64Run ld_cg(const F64Run* p) {
-    // 24-byte records are only 8-byte aligned: three 8-byte loads
+    // 16-byte records, 8-byte aligned: two 8-byte loads
     const double a = __ldcg(reinterpret_cast<const double*>(p));
     const float2 t = __ldcg(reinterpret_cast<const float2*>(reinterpret_cast<const char*>(p) + 8));
-    const float2 u = __ldcg(reinterpret_cast<const float2*>(reinterpret_cast<const char*>(p) + 16));
-    return {a, t.x, t.y, u.x, u.y};
+    return {a, t.x, t.y};
 }
 __device__ __forceinline__ F32Pair ld_cg(const F32Pair* p) {
     const float2 t = __ldcg(reinterpret_cast<const float2*>(p));

@@ -176,15 +176,15 @@ template <int NP> struct PackedF32C {
 template <> struct VecAcc<AddF32C, 2> : PackedF32C<1> {};
 template <> struct VecAcc<AddF32C, 4> : PackedF32C<2> {};
 
-// float64 as float pairs, columns in pairs: double run folds, float2 (hi, lo, plain-sum) state.
+// float64 as float pairs, columns in pairs: double run folds, float2 (hi, lo) state.
 template <int NP> struct PackedF64S {
     double acc[2 * NP];
-    float2 hi[NP], lo[NP], p[NP];
+    float2 hi[NP], lo[NP];
     __device__ __forceinline__ void zero() {
 #pragma unroll
         for (int j = 0; j < NP; j++) {
             acc[2 * j] = acc[2 * j + 1] = 0.0;
-            hi[j] = lo[j] = p[j] = make_float2(0.0f, 0.0f);
+            hi[j] = lo[j] = make_float2(0.0f, 0.0f);
         }
     }
     __device__ __forceinline__ void add(const DF* v) {
@@ -196,7 +196,6 @@ template <int NP> struct PackedF64S {
             two_sum2(hi[j], xh, s, e);
             lo[j] = add2(lo[j], add2(e, xl));
             hi[j] = s;
-            p[j] = add2(p[j], xh);
         }
     }
     template <int N> __device__ __forceinline__ void add_block(const DF (*v)[2 * NP]) {
@@ -215,18 +214,16 @@ template <int NP> struct PackedF64S {
         }
     }
     __device__ __forceinline__ F64Run get(int i) const {
-        return {acc[i], lane_of(hi[i >> 1], i), lane_of(lo[i >> 1], i), lane_of(p[i >> 1], i), 0.0f};
+        return {acc[i], lane_of(hi[i >> 1], i), lane_of(lo[i >> 1], i)};
     }
     __device__ __forceinline__ void set(int i, const F64Run& r) {
         acc[i] = r.acc;
         if (i & 1) {
             hi[i >> 1].y = r.hi;
             lo[i >> 1].y = r.lo;
-            p[i >> 1].y = r.p;
         } else {
             hi[i >> 1].x = r.hi;
             lo[i >> 1].x = r.lo;
-            p[i >> 1].x = r.p;
         }
     }
     __device__ __forceinline__ void flush() {
@@ -258,7 +255,6 @@ template <int NP> struct PackedF64S {
             r.acc[2 * j + 1] = __shfl_xor_sync(FULL_MASK, acc[2 * j + 1], m);
             r.hi[j] = shfl_xor2(hi[j], m);
             r.lo[j] = shfl_xor2(lo[j], m);
-            r.p[j] = shfl_xor2(p[j], m);
         }
         return r;
     }
@@ -270,7 +266,6 @@ template <int NP> struct PackedF64S {
             r.acc[2 * j + 1] = __shfl_up_sync(FULL_MASK, acc[2 * j + 1], d);
             r.hi[j] = shfl_up2(hi[j], d);
             r.lo[j] = shfl_up2(lo[j], d);
-            r.p[j] = shfl_up2(p[j], d);
         }
         return r;
     }
