@@ -33,11 +33,6 @@ struct DevCSR {
 struct DevicePlan {
     int device = -1;
     DevCSR up, down, seed, miss;
-    // UP's first level (height 1) cut by blocks of `up1b_block` consecutive height-0 ids: level j
-    // of up1b holds, for every height-1 node with children in block j, those children.  Empty
-    // when the graph has fewer than two blocks.
-    DevCSR up1b;
-    long long up1b_block = 0, up1b_src = 0, up1b_node_begin = 0, up1b_node_end = 0;
     uint32_t* mut_new = nullptr;
     uint32_t* miss_new = nullptr;
     uint32_t* old2new = nullptr;
@@ -84,21 +79,9 @@ int sm_count();
 // Launches one level of a CSR (a no-op when the level has no chunks); `work` points at
 // `tileStride` (0: L.ntiles) zeroed counters owned by this launch, and the heavy-row tickets
 // are `tileStride` apart.  `shape` null: the default shape.  Returns the kernels launched.
-// `state` set: each row's sum is merged into its Op::A accumulator at state + (node - stateBase)
-// rows instead of being written (one pass of a sample-blocked level).
 int launch_level(const Layout& L, const DevCSR& c, size_t level, const void* src, void* dst, int rmw,
                  void* partials, unsigned* tickets, unsigned* work, cudaStream_t s, const int* gate = nullptr,
-                 int gateValue = 0, const LevelShape* shape = nullptr, int tileStride = 0, void* state = nullptr,
-                 long long stateBase = 0);
-
-// Sample-blocked passes of the UP CSR's first level (blocked.cu): finishes the accumulated state
-// of nodes [node_begin, node_end) into their values (added onto them when rmw).
-void launch_state_finish(Kind kind, const void* state, void* vals, long long node_begin, long long node_end,
-                         long long stride, int rmw, cudaStream_t s, const int* gate, int gateValue);
-// Source-row bytes above which UP's first level runs in sample-blocked passes, and the block size
-// (in height-0 ids) the plan is cut into; both adjustable for tests.
-uint64_t blocked_threshold_bytes();
-long long blocked_block_size();
+                 int gateValue = 0, const LevelShape* shape = nullptr, int tileStride = 0);
 
 // Builds (once) and returns the graph's plan on the current device.
 DevicePlan* ensure_device_plan(grgx_graph* g);

@@ -172,8 +172,6 @@ SweepParams<S> make_params(const DevCSR& c, long long cb, long long ce, const vo
     p.ntiles = ntiles;
     p.gate = nullptr;
     p.gate_value = 0;
-    p.state = nullptr;
-    p.state_base = 0;
     return p;
 }
 
@@ -181,7 +179,7 @@ SweepParams<S> make_params(const DevCSR& c, long long cb, long long ce, const vo
 // `work` points at L.ntiles zeroed counters owned by this launch.
 int launch_level(const Layout& L, const DevCSR& c, size_t level, const void* src, void* dst, int rmw,
                  void* partials, unsigned* tickets, unsigned* work, cudaStream_t s, const int* gate,
-                 int gateValue, const LevelShape* shape, int tileStride, void* state, long long stateBase) {
+                 int gateValue, const LevelShape* shape, int tileStride) {
     const long long cb = c.lb[level], ce = c.le[level];
     if (ce <= cb) return 0;
     const LevelShape sh = shape ? *shape : default_shape(L);
@@ -194,8 +192,6 @@ int launch_level(const Layout& L, const DevCSR& c, size_t level, const void* src
         SweepParams<S> p = make_params<S>(c, cb, ce, src, dst, L.stride, rmw, partials, tickets, work, ts);
         p.gate = gate;
         p.gate_value = gateValue;
-        p.state = state;
-        p.state_base = stateBase;
         return p;
     };
     const int vw = L.vw, g = sh.g, v = sh.variant;
@@ -231,7 +227,6 @@ uint32_t* build_plan_device(const HostGraph& g, const unsigned long long* dOff, 
                             HostPlan& plan);
 
 void decode_edges_device(const HostGraph& hg, void** dOff, void** dAdj);
-void build_up_blocked(DevicePlan& d, const HostPlan& hp);
 
 namespace {
 // The E-sized passes of the plan on the device (plan_device.cu) from the down CSR, uploaded
@@ -309,7 +304,6 @@ DevicePlan* ensure_device_plan(grgx_graph* g) {
     d->has_miss = hp.has_miss;
     for (uint32_t x : hp.xtx_new)
         if (x != COAL_NOT_SET) d->xtx_max = std::max(d->xtx_max, static_cast<double>(x));
-    build_up_blocked(*d, hp);
     g->dev = std::move(d);
     g->plan.reset();  // the device copy is authoritative; free the host copy
     return g->dev.get();
@@ -423,21 +417,12 @@ void matmul_direct(grgx_graph* g, int dtype, const void* input, uint64_t in_cols
         // ---- node values and the per-call scratch ---------------------------------------------
         const size_t valBytes = static_cast<size_t>(n) * L.stride * L.ssize;
         void* vals = sc.get(valBytes);
-        // UP's first level in sample-blocked passes when the height-0 rows outgrow L2
-        const bool blocked = !down && dp->up1b.n_rows > 0 &&
-                             static_cast<uint64_t>(dp->up1b_src) * static_cast<uint64_t>(L.stride) * L.ssize >
-                                 blocked_threshold_bytes();
         long long pieces = down ? std::max(dp->down.n_pieces, std::max(dp->seed.n_pieces, dp->miss.n_pieces))
-                                : std::max(dp->up.n_pieces, blocked ? dp->up1b.n_pieces : 0ll);
+                                : dp->up.n_pieces;
         void* partials = sc.get(static_cast<size_t>(pieces) * L.stride * L.asize);
-        const long long nh = down ? (dp->down.n_heavy + dp->seed.n_heavy + dp->miss.n_heavy)
-                                  : dp->up.n_heavy + (blocked ? dp->up1b.n_heavy : 0);
+        const long long nh = down ? (dp->down.n_heavy + dp->seed.n_heavy + dp->miss.n_heavy) : dp->up.n_heavy;
         const long long nslots = down ? (2 + static_cast<long long>(dp->down.lb.size()))
-                                      : static_cast<long long>(dp->up.lb.size() + (blocked ? dp->up1b.lb.size() : 0));
-        void* state = nullptr;
-        if (blocked)
-            state = sc.get(static_cast<size_t>(dp->up1b_node_end - dp->up1b_node_begin) * L.stride *
-                           std::max(L.asize, 8));
+                                      : static_cast<long long>(dp->up.lb.size());
         // counters per launch and per heavy row: enough column tiles for any launch shape
         const int TS = max_tiles(L);
         const size_t counterBytes = static_cast<size_t>(nh + nslots) * TS * sizeof(unsigned);
@@ -556,24 +541,8 @@ void matmul_direct(grgx_graph* g, int dtype, const void* input, uint64_t in_cols
                 // UP seed: samples <- input columns
                 load_rows(dIn, in_cols, N, by_indiv ? MAP_DIV : MAP_IDENT, P, nullptr, vals, hasInit);
                 if (timed && t_timing) GRGX_CUDA(cudaEventRecord(ev[1], s));
-                for (size_t lvl = 0; lvl < dp->up.lb.size(); lvl++) {
-                    if (lvl == 0 && blocked) {
-                        const long long nb0 = dp->up1b_node_begin, nb1 = dp->up1b_node_end;
-                        GRGX_CUDA(cudaMemsetAsync(state, 0,
-                                                  static_cast<size_t>(nb1 - nb0) * LL.stride * std::max(LL.asize, 8), s));
-                        unsigned* bt = tickets + dp->up.n_heavy * TS;
-                        unsigned* bw = work + dp->up.lb.size() * TS;
-                        for (size_t j = 0; j < dp->up1b.lb.size(); j++) {
-                            const LevelShape sh = level_shape(LL, dp->up1b, j);
-                            launches += launch_level(LL, dp->up1b, j, vals, vals, 0, partials, bt, bw + j * TS, s, g,
-                                                     gv, &sh, TS, state, nb0);
-                        }
-                        launch_state_finish(LL.kind, state, vals, nb0, nb1, LL.stride, hasInit, s, g, gv);
-                        launches++;
-                        continue;
-                    }
+                for (size_t lvl = 0; lvl < dp->up.lb.size(); lvl++)
                     launches += level(dp->up, lvl, vals, hasInit, tickets, work + lvl * TS);
-                }
                 if (timed && t_timing) GRGX_CUDA(cudaEventRecord(ev[2], s));
                 if (emit_all) {
                     store_cols(n, MAP_TABLE, 1, dp->old2new, dOut, out_cols, add);

@@ -49,8 +49,6 @@ template <typename S> struct SweepParams {
     int ntiles;
     const int* gate;           // when set, the launch runs only if *gate == gate_value
     int gate_value;
-    void* state;               // when set: merge each row sum into Op::A state (sample-blocked passes)
-    long long state_base;      // node id of the first state row
 };
 
 template <typename S, int VW> struct Vec;
@@ -82,6 +80,25 @@ template <class Op, int VW, int G> __device__ __forceinline__ void group_allredu
     }
 }
 
+template <class Op, int VW>
+__device__ __forceinline__ void write_row(const SweepParams<typename Op::S>& p, long long row, int col,
+                                          const VecAcc<Op, VW>& tot) {
+    using S = typename Op::S;
+    const long long node = p.rows[row];
+    S* d = p.dst + node * p.stride + col;
+    S out[VW];
+    if (p.rmw) {
+        S base[VW];
+        ld_plain<S, VW>(d, base);
+#pragma unroll
+        for (int i = 0; i < VW; i++) out[i] = Op::finish_onto(base[i], tot.get(i));
+    } else {
+#pragma unroll
+        for (int i = 0; i < VW; i++) out[i] = Op::finish(tot.get(i));
+    }
+    Vec<S, VW>::st(d, out);
+}
+
 // L2-coherent loads for the heavy-row partials written by other warps of the same launch.
 __device__ __forceinline__ uint32_t ld_cg(const uint32_t* p) { return __ldcg(p); }
 __device__ __forceinline__ unsigned long long ld_cg(const unsigned long long* p) { return __ldcg(p); }
@@ -96,37 +113,6 @@ __device__ __forceinline__ F64Run ld_cg(const F64Run* p) {
 __device__ __forceinline__ F32Pair ld_cg(const F32Pair* p) {
     const float2 t = __ldcg(reinterpret_cast<const float2*>(p));
     return {t.x, t.y};
-}
-
-template <class Op, int VW>
-__device__ __forceinline__ void write_row(const SweepParams<typename Op::S>& p, long long row, int col,
-                                          const VecAcc<Op, VW>& tot) {
-    using S = typename Op::S;
-    const long long node = p.rows[row];
-    if (p.state != nullptr) {
-        // a pass over one block of source rows: the row's running sum stays in accumulator form
-        using A = typename Op::A;
-        A* st = static_cast<A*>(p.state) + (node - p.state_base) * p.stride + col;
-#pragma unroll
-        for (int i = 0; i < VW; i++) {
-            A cur = ld_cg(st + i);
-            Op::merge(cur, tot.get(i));
-            st[i] = cur;
-        }
-        return;
-    }
-    S* d = p.dst + node * p.stride + col;
-    S out[VW];
-    if (p.rmw) {
-        S base[VW];
-        ld_plain<S, VW>(d, base);
-#pragma unroll
-        for (int i = 0; i < VW; i++) out[i] = Op::finish_onto(base[i], tot.get(i));
-    } else {
-#pragma unroll
-        for (int i = 0; i < VW; i++) out[i] = Op::finish(tot.get(i));
-    }
-    Vec<S, VW>::st(d, out);
 }
 
 // Accumulators may bound their running chains: AddF64S renormalises its float pair every 4
