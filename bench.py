@@ -316,6 +316,14 @@ def large_graph(gx, torch, args, peak):
     stats = graph_stats(g)
     stats["device_bytes"] = g.info()["device_bytes"]
     E = stats["edges"]
+    t_tune = 0.0
+    if not args.no_autotune:
+        t0 = time.perf_counter()
+        for K in (16, 64, 256):
+            for dt in ("float64", "float32"):
+                for d in (UP, DOWN):
+                    gx.autotune(g, dt, K, d)
+        t_tune = time.perf_counter() - t0
     rng = np.random.default_rng(5)
     rows = []
     gx.set_timing(True)
@@ -355,7 +363,7 @@ def large_graph(gx, torch, args, peak):
     return {"graph": dict(stats, note=f"variant prefix M'={args.large_mutations} of the 10,000,000-variant "
                                       "generator run, sized to the 2-4e9-edge budget"),
             "edgeK_per_s": units / secs, "alg_GBps": abytes / secs / 1e9, "hbm_frac": abytes / secs / 1e9 / peak,
-            "matmuls": rows, "setup_s": {"generate": t_gen, "plan_upload": t_up}}
+            "matmuls": rows, "setup_s": {"generate": t_gen, "plan_upload": t_up, "autotune": t_tune}}
 
 
 def run_reference(args):

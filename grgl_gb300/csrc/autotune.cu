@@ -6,9 +6,11 @@
 // SM less).  Which is fastest depends on the level's width (rows), its mean degree (edges per
 // row) and K, so the table is keyed on
 //     (storage kind, row stride in elements, floor(log2(rows + 1)), floor(log2(edges / rows + 1)))
-// and filled by measuring: grgx_autotune times every candidate on each level of one traversal
-// of a resident graph (CUDA events around the level's launch, best of three) and records the
-// winner when it beats the default by more than 2%.  Calls on any graph then look up every
+// and filled by measuring: grgx_autotune times candidates on each level of one traversal of a
+// resident graph (CUDA events around the level's launch, best of two after a warm launch) --
+// the deep variant at the default lanes, then halvings of the lanes per row while each keeps
+// winning -- and records the winner when it beats the default by more than 2%.  Levels with
+// under 0.5% of the traversal's edges keep the default.  Calls on any graph then look up every
 // level's key; levels without an entry run the default shape.  Shapes change only the order in
 // which a row's float terms are added (integer results are bit-exact with any shape).
 #include <cuda_runtime.h>
@@ -129,7 +131,7 @@ void autotune_import(const std::string& text) {
 
 void clear_graph_replays(grgx_graph* g);
 
-// Times every candidate shape on each level of one traversal in `direction` and records the
+// Times the candidate shapes on each level of one traversal in `direction` and records the
 // winners.  The values swept are zeros: the gathers, the edge walk and the arithmetic do not
 // depend on them.
 std::string autotune_impl(grgx_graph* g, int dtype, uint64_t rows, int direction, uint32_t flags) {
@@ -172,7 +174,7 @@ std::string autotune_impl(grgx_graph* g, int dtype, uint64_t rows, int direction
         const int rmw = down ? 1 : 0;
         auto time_shape = [&](size_t lvl, const LevelShape& sh) {
             float best = 1e30f;
-            for (int rep_i = 0; rep_i < 4; rep_i++) {
+            for (int rep_i = 0; rep_i < 3; rep_i++) {
                 GRGX_CUDA(cudaMemsetAsync(counters, 0, counterBytes, s));
                 GRGX_CUDA(cudaEventRecord(e0, s));
                 launch_level(L, c, lvl, vals, vals, rmw, partials, tickets, work, s, nullptr, 0, &sh, maxT);
@@ -185,29 +187,32 @@ std::string autotune_impl(grgx_graph* g, int dtype, uint64_t rows, int direction
             }
             return best;
         };
-        std::vector<LevelShape> cands;
-        for (int gg : candidate_g(L)) {
-            cands.push_back(LevelShape{gg, tiles_for(L, gg), 0});
-            if (has_deep(L)) cands.push_back(LevelShape{gg, tiles_for(L, gg), 1});
-        }
+        const std::vector<int> gs = candidate_g(L);
         double totDefault = 0, totBest = 0;
         for (size_t lvl = 0; lvl < c.lb.size(); lvl++) {
             if (c.le[lvl] <= c.lb[lvl]) continue;
+            // levels under 0.5% of the traversal's edges keep the default untimed
+            if (c.level_edges[lvl] * 200 < c.n_edges) continue;
             const LevelShape def = default_shape(L);
             const float tDef = time_shape(lvl, def);
             LevelShape best = def;
             float tBest = tDef;
-            for (const LevelShape& sh : cands) {
-                if (sh.g == def.g && sh.variant == def.variant) continue;
-                const float t = time_shape(lvl, sh);
-                if (t < tBest) {
+            // greedy: the deep variant at the default lanes, then fewer lanes per row with the
+            // better variant while each halving keeps winning by 2%
+            if (has_deep(L)) {
+                const LevelShape deep{def.g, def.ntiles, 1};
+                const float t = time_shape(lvl, deep);
+                if (t < 0.98f * tBest) {
                     tBest = t;
-                    best = sh;
+                    best = deep;
                 }
             }
-            if (tBest > 0.98f * tDef) {
-                best = def;
-                tBest = tDef;
+            for (size_t i = 1; i < gs.size(); i++) {
+                const LevelShape sh{gs[i], tiles_for(L, gs[i]), best.variant};
+                const float t = time_shape(lvl, sh);
+                if (!(t < 0.98f * tBest)) break;
+                tBest = t;
+                best = sh;
             }
             totDefault += tDef;
             totBest += tBest;

@@ -263,10 +263,12 @@ void grgx_host_free(void* p);
  * process-wide table is keyed on (storage kind, row stride, log2 of the level's rows, log2 of
  * its mean degree); levels without an entry run the default shape.
  *
- * grgx_autotune times every candidate on each level of one traversal of `g` (resident on the
+ * grgx_autotune times candidates on each level of one traversal of `g` (resident on the
  * current device; it is uploaded first) for `rows` x cols inputs of `dtype` in `direction`
  * (`flags`: GRGX_FLAG_F32_PLAIN / GRGX_FLAG_F64_NATIVE select the accumulator as in
- * grgx_matmul), records each level's winner when it beats the default by more than 2%, and
+ * grgx_matmul): the deep variant, then fewer lanes per row while that keeps winning; levels
+ * with under 0.5% of the edges keep the default.  It records each level's winner when it beats
+ * the default by more than 2%, and
  * writes a per-level report to `report` (NUL-terminated, truncated to `report_len`;
  * `report_needed`, if not NULL, gets the full size).  It drops `g`'s captured CUDA graphs; make
  * no other call on `g` while it runs.  Float results may round differently under another shape
