@@ -455,8 +455,10 @@ def main():
         for dt, K, d in dict.fromkeys(combos):
             levels_tuned += gx.autotune(g, dt, K, d).count("level ")
         torch.cuda.synchronize()
+        table = gx.autotune_table()
         tune = {"seconds": time.perf_counter() - t0, "levels_tuned": levels_tuned,
-                "table_entries": len(gx.autotune_table().strip().splitlines())}
+                "table_entries": len(table.strip().splitlines())}
+        print("autotune table (kind stride rows_log2 degree_log2 g tiles variant):\n" + table, file=sys.stderr)
 
     # warm-up
     for _ in range(args.warmup):
