@@ -58,7 +58,7 @@ def cases_for(N: int, M: int, n: int, ploidy: int, has_miss: bool = False, profi
     add("up_i32_ones_k1", np.int32, 1, UP, ones=True)
     add("down_f64_k1", np.float64, 1, DOWN)
     add("up_f64_k1", np.float64, 1, UP)
-    if profile == "cfg1":
+    if profile == "wt_n1000_m10000":
         return out
     if has_miss:
         add("down_f64_miss_k2", np.float64, 2, DOWN, miss="input")

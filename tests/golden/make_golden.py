@@ -11,7 +11,7 @@ Produces, next to this script:
                               the UP int32 ones output is checked against the reference's own golden
                               allele counts, test/endtoend/expect/test-200-samples.freq.txt
   t200miss.grg / t200miss.npz the same for test-200-samples.miss.igd (missingness nodes, `miss`)
-  cfg1.grg / cfg1.npz         the seeded window-tree genotypes (N=1,000 haplotypes, M=10,000 variants,
+  wt_n1000_m10000.grg / wt_n1000_m10000.npz         the seeded window-tree genotypes (N=1,000 haplotypes, M=10,000 variants,
                               seed 42) written as VCF and built by the reference constructor, with the
                               reference outputs of DOWN int32 ones, DOWN f64 N(0,1) and UP f64 N(0,1)
 Inputs are regenerated in the tests from the seeds stored in each .npz.
@@ -102,11 +102,11 @@ def main():
                             mut_node=a["mut_node"])
     X = og.dense_X().astype(np.int8)
     assert X.max() <= 1, "window-tree genotypes must be 0/1"
-    vcf = Path("/tmp/grgx_cfg1.vcf.gz")
+    vcf = Path("/tmp/grgx_wt_n1000_m10000.vcf.gz")
     write_vcf(X, vcf)
-    construct(vcf, HERE / "cfg1.grg")
-    record(HERE / "cfg1.grg", HERE / "cfg1.npz", {"generator": "window_tree N=1000 M=10000 seed=42 window=100",
-                                                  "nnz": int(X.sum())}, "cfg1")
+    construct(vcf, HERE / "wt_n1000_m10000.grg")
+    record(HERE / "wt_n1000_m10000.grg", HERE / "wt_n1000_m10000.npz", {"generator": "window_tree N=1000 M=10000 seed=42 window=100",
+                                                  "nnz": int(X.sum())}, "wt_n1000_m10000")
 
 
 if __name__ == "__main__":

@@ -31,7 +31,7 @@ def test_exports_every_declared_symbol(lib_built):
     assert declared == set(_lib.SIGNATURES), declared ^ set(_lib.SIGNATURES)
 
 
-@pytest.mark.parametrize("fixture", ["t200", "t200miss", "cfg1"])
+@pytest.mark.parametrize("fixture", ["t200", "t200miss", "wt_n1000_m10000"])
 def test_loader_matches_independent_reader(gx, fixture):
     g = gx.load_immutable_grg(str(GOLDEN / f"{fixture}.grg"))
     o = oracle.read_grg(GOLDEN / f"{fixture}.grg")
@@ -146,11 +146,11 @@ def test_window_tree_generator_structure(gx):
 
 def test_window_tree_equals_reference_construction(gx):
     """The directly emitted graph and the reference constructor's graph for the same genotypes
-    (tests/golden/cfg1.grg, built from the generator's VCF) give identical integer products."""
+    (tests/golden/wt_n1000_m10000.grg, built from the generator's VCF) give identical integer products."""
     direct = gx.window_tree_grg(1000, 10000, seed=42).export_arrays()
     og = oracle.OracleGraph(num_samples=1000, ploidy=2, down_off=direct["down_off"], down_adj=direct["down_adj"],
                             mut_node=direct["mut_node"])
-    ref = oracle.read_grg(GOLDEN / "cfg1.grg")
+    ref = oracle.read_grg(GOLDEN / "wt_n1000_m10000.grg")
     rng = np.random.default_rng(11)
     for direction, cols in ((UP, 1000), (DOWN, 10000)):
         V = rng.integers(-1000, 1000, size=(2, cols)).astype(np.int64)

@@ -48,7 +48,7 @@ def test_kats_on_gpu(gx):
     assert np.array_equal(gx.matmul(g8, np.eye(8, dtype=np.int64), UP), og8.dense_X())
 
 
-@pytest.mark.parametrize("fixture", ["t200", "t200miss", "cfg1"])
+@pytest.mark.parametrize("fixture", ["t200", "t200miss", "wt_n1000_m10000"])
 def test_reference_golden_outputs(gx, fixture):
     z, meta = load_golden(fixture)
     g = gx.load_immutable_grg(str(GOLDEN / f"{fixture}.grg"))

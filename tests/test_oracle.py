@@ -81,7 +81,7 @@ def test_kat_sample8_dense():
     assert np.array_equal(oracle.matmul(g, np.eye(6, dtype=np.int64), DOWN), X.T)
 
 
-@pytest.mark.parametrize("fixture", ["t200", "t200miss", "cfg1"])
+@pytest.mark.parametrize("fixture", ["t200", "t200miss", "wt_n1000_m10000"])
 def test_oracle_matches_reference_golden(fixture):
     """The restatement reproduces the reference's outputs bit for bit (same summation order)."""
     from tests.conftest import GOLDEN
@@ -114,7 +114,7 @@ def test_golden_freq_pin():
 def test_sharded_oracle_matches_plain():
     from tests.conftest import GOLDEN
 
-    g = oracle.read_grg(GOLDEN / "cfg1.grg")
+    g = oracle.read_grg(GOLDEN / "wt_n1000_m10000.grg")
     rng = np.random.default_rng(3)
     sh = oracle.Shards(g, 4)
     for direction, cols in ((UP, g.num_samples), (DOWN, g.num_mutations)):

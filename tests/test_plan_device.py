@@ -78,7 +78,7 @@ def test_kat_graph_device_plan(gx):
     assert np.array_equal(gx.matmul(g, V, UP), oracle.matmul(og, V, UP))
 
 
-@pytest.mark.parametrize("fixture", ["t200", "t200miss", "cfg1"])
+@pytest.mark.parametrize("fixture", ["t200", "t200miss", "wt_n1000_m10000"])
 def test_grg_decoded_on_device(gx, fixture):
     """A .grg's buckets decoded on the GPU give the plan (and every product) of the same file
     decoded on the host."""
