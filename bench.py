@@ -56,6 +56,7 @@ def parse_args():
     ap.add_argument("--serve-requests", type=int, default=96, help="most arrivals in a served run")
     ap.add_argument("--no-large", action="store_true", help="skip the large-graph measurement")
     ap.add_argument("--no-autotune", action="store_true", help="run the default launch shapes (no tuning pass)")
+    ap.add_argument("--no-load", action="store_true", help="skip the .grg save / cold-load measurement")
     ap.add_argument("--large-samples", type=int, default=1_000_000)
     ap.add_argument("--large-mutations", type=int, default=300_000)
     return ap.parse_args()
@@ -298,6 +299,35 @@ def served(gx, graphs, rate, seconds, max_requests, rng):
             "p50_ms": float(np.percentile(lat_ms, 50)), "p99_ms": float(np.percentile(lat_ms, 99)),
             "served_edgeK_per_s": units / t_served, "plain_sequential_edgeK_per_s": units / t_plain,
             "mean_batch_requests": float(np.mean(batches))}
+
+
+def cold_start(gx, torch, g):
+    """Serving cold start: the graph written as a .grg file, then read back (edge buckets kept
+    encoded) and made resident (buckets decoded on the GPU, plan built on the GPU)."""
+    fd, path = tempfile.mkstemp(suffix=".grg")
+    os.close(fd)
+    try:
+        t0 = time.perf_counter()
+        g.save(path)
+        t_save = time.perf_counter() - t0
+        size = os.path.getsize(path)
+        t0 = time.perf_counter()
+        g2 = gx.load_immutable_grg(path)
+        t_load = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        g2.upload()
+        torch.cuda.synchronize()
+        t_up = time.perf_counter() - t0
+        same = g2.info()["device_bytes"] == g.info()["device_bytes"]
+        del g2
+        torch.cuda.empty_cache()
+        return {"file_bytes": size, "edges": g.num_edges, "save_s": t_save, "read_s": t_load,
+                "decode_and_plan_on_gpu_s": t_up, "load_to_resident_s": t_load + t_up, "same_plan_size": same}
+    except (OSError, RuntimeError) as e:
+        return {"unavailable": str(e)}
+    finally:
+        if os.path.exists(path):
+            os.unlink(path)
 
 
 def large_graph(gx, torch, args, peak):
@@ -544,6 +574,10 @@ def main():
         e2e_value = units_per_step * e2e_steps * world / e2e_s
         del pinned_inputs
 
+    cold = None
+    if rank == 0 and not args.no_load:
+        cold = cold_start(gx, torch, g)
+
     batched = serve = large = None
     if rank == 0 and not args.no_serve:
         rng2 = np.random.default_rng(11)
@@ -599,6 +633,7 @@ def main():
             "batched_vs_plain": batched,
             "served": serve,
             "large_graph": large,
+            "cold_start": cold,
             "autotune": tune,
             "setup_s": {"generate": t_gen, "plan_upload": t_up},
         }

@@ -48,6 +48,7 @@ SIGNATURES = {
     "grgx_graph_load": (_int, [ctypes.c_char_p, ctypes.POINTER(c_graph_p)]),
     "grgx_graph_from_csr": (_int, [_u64, _u64, _u64, _vp, _vp, _u64, _vp, _vp, _vp, ctypes.POINTER(c_graph_p)]),
     "grgx_graph_generate": (_int, [_u64, _u64, _u64, _u32, _int, ctypes.POINTER(c_graph_p)]),
+    "grgx_graph_save": (_int, [c_graph_p, ctypes.c_char_p]),
     "grgx_graph_destroy": (None, [c_graph_p]),
     "grgx_graph_subset": (_int, [c_graph_p, _vp, _u64, ctypes.POINTER(c_graph_p)]),
     "grgx_graph_info_get": (_int, [c_graph_p, ctypes.POINTER(GraphInfo)]),

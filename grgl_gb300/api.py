@@ -108,6 +108,10 @@ class GRG:
         _lib.check(_lib.lib().grgx_graph_info_get(self._h, ctypes.byref(info)))
         return {name: int(getattr(info, name)) for name, _ in info._fields_}
 
+    def save(self, path: str) -> None:
+        """Write the graph as a .grg file (pygrgl.save_grg without simplification)."""
+        _lib.check(_lib.lib().grgx_graph_save(self._h, str(path).encode()))
+
     def upload(self) -> "GRG":
         """Build the level plan and make it resident on the current CUDA device."""
         _lib.check(_lib.lib().grgx_graph_upload(self._h))

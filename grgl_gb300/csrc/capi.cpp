@@ -210,6 +210,13 @@ grgx_status grgx_graph_subset(const grgx_graph* g, const uint32_t* mutation_ids,
     });
 }
 
+grgx_status grgx_graph_save(const grgx_graph* g, const char* path) {
+    return guarded([&] {
+        GRGX_CHECK(g && path, GRGX_ERR_API_MISUSE, "null argument");
+        save_grg_file(const_cast<grgx_graph*>(g)->host_edges(), path);
+    });
+}
+
 void grgx_graph_destroy(grgx_graph* g) {
     if (!g) return;
     try {

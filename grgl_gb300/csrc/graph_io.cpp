@@ -18,9 +18,11 @@
 //   missingness nodes, if flag 0x4: u32 x mutations
 // The varint format is LEB128-style: 7 data bits per byte, high bit = more bytes follow
 // (third-party/libvbyte/vbyte.cc:98-147).
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <fstream>
+#include <thread>
 
 #include "grgx_internal.h"
 
@@ -169,6 +171,112 @@ std::unique_ptr<HostGraph> load_grg_file(const std::string& path) {
             GRGX_CHECK(n == INVALID_NODE || n < h.nodeCount, GRGX_ERR_BAD_FILE, "Malformed GRG file");
     }
     return g;
+}
+
+namespace {
+void put_varint(std::vector<uint8_t>& out, uint32_t v) {
+    while (v >= 0x80u) {
+        out.push_back(static_cast<uint8_t>(v | 0x80u));
+        v >>= 7;
+    }
+    out.push_back(static_cast<uint8_t>(v));
+}
+}  // namespace
+
+// Writes format 5.3 in the layout the reader above takes (the reference writer's order,
+// serialize.cpp:517-669): header; edge bucket bytes and buckets (count + deltas of the ascending
+// children, an empty bucket for a node without children); u64 bucket offsets; mutation nodes;
+// 24-byte mutation records (REF "A", ALT "C" stored inline, time not set); coalescence counts;
+// missingness nodes when present.  Children must be ascending within each node.
+void save_grg_file(const HostGraph& g, const std::string& path) {
+    const uint64_t n = g.num_nodes, M = g.num_mutations;
+    // buckets encoded in parallel over node ranges balanced by edge count, then concatenated
+    const uint64_t E = g.down_adj.size();
+    const unsigned hw = std::thread::hardware_concurrency();
+    const int T = (E < (1u << 22)) ? 1 : static_cast<int>(std::min(64u, hw ? hw : 4u));
+    std::vector<uint64_t> nb(T + 1, n);
+    nb[0] = 0;
+    for (int t = 1; t < T; t++)
+        nb[t] = static_cast<uint64_t>(std::lower_bound(g.down_off.begin(), g.down_off.end(), E * t / T) -
+                                      g.down_off.begin());
+    std::vector<std::vector<uint8_t>> part(T);
+    std::vector<uint64_t> index(n + 1, 0);
+    std::vector<int> bad(T, 0);
+    auto encode = [&](int t) {
+        std::vector<uint8_t>& out = part[t];
+        for (uint64_t v = nb[t]; v < nb[t + 1]; v++) {
+            index[v] = out.size();  // relative to the part; rebased below
+            const uint64_t b = g.down_off[v], e = g.down_off[v + 1];
+            if (b < e) {
+                put_varint(out, static_cast<uint32_t>(e - b));
+                uint32_t prev = 0;
+                for (uint64_t x = b; x < e; x++) {
+                    const uint32_t c = g.down_adj[x];
+                    if (x != b && c < prev) bad[t] = 1;
+                    put_varint(out, c - prev);
+                    prev = c;
+                }
+            }
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 1; t < T; t++) pool.emplace_back(encode, t);
+    encode(0);
+    for (auto& th : pool) th.join();
+    for (int t = 0; t < T; t++) GRGX_CHECK(!bad[t], GRGX_ERR_API_MISUSE, "children must be ascending to be saved");
+    uint64_t base = 0;
+    for (int t = 0; t < T; t++) {
+        for (uint64_t v = nb[t]; v < nb[t + 1]; v++) index[v] += base;
+        base += part[t].size();
+    }
+    index[n] = base;
+    FileHeader h{};
+    h.magic = FILE_MAGIC;
+    h.versionMajor = FILE_MAJOR;
+    h.versionMinor = 3;
+    h.ploidy = static_cast<uint16_t>(g.ploidy);
+    h.populationCount = 0;
+    h.sampleCount = g.num_samples;
+    h.mutationCount = M;
+    h.nodeCount = n;
+    h.edgeCount = g.down_adj.size();
+    uint64_t lo = UINT64_MAX, hi = 0;
+    for (uint64_t p : g.mut_pos) {
+        lo = std::min(lo, p);
+        hi = std::max(hi, p + 1);
+    }
+    h.rangeStart = g.mut_pos.empty() ? 0 : lo;
+    h.rangeEnd = g.mut_pos.empty() ? 0 : hi;
+    h.flags = (g.phased ? 0 : FLAG_UNPHASED) | (g.miss_node.empty() ? 0 : FLAG_HAS_MISSING);
+    std::ofstream out(path, std::ios::binary | std::ios::trunc);
+    GRGX_CHECK(out.good(), GRGX_ERR_API_MISUSE, "Could not write " + path);
+    auto put = [&](const void* p, size_t bytes) {
+        out.write(static_cast<const char*>(p), static_cast<std::streamsize>(bytes));
+    };
+    put(&h, sizeof(h));
+    const uint64_t edgeBytes = base;
+    put(&edgeBytes, sizeof(edgeBytes));
+    for (int t = 0; t < T; t++) put(part[t].data(), part[t].size());
+    put(index.data(), index.size() * sizeof(uint64_t));
+    put(g.mut_node.data(), g.mut_node.size() * sizeof(uint32_t));
+    for (uint64_t m = 0; m < M; m++) {
+        uint8_t rec[24] = {0};
+        rec[1] = 'A';  // byte 0 stays 0: alleles stored inline
+        rec[2] = 'C';
+        const uint64_t pos = m < g.mut_pos.size() ? g.mut_pos[m] : m + 1;
+        const uint32_t timeNotSet = 0x3FFFFFFFu;
+        const uint16_t altIndex = 1;
+        std::memcpy(rec + 8, &pos, 8);
+        std::memcpy(rec + 16, &timeNotSet, 4);
+        std::memcpy(rec + 20, &altIndex, 2);
+        put(rec, sizeof(rec));
+    }
+    std::vector<uint32_t> coals(n - g.num_samples, COAL_NOT_SET);
+    for (size_t i = 0; i < coals.size() && i < g.coals.size(); i++) coals[i] = g.coals[i];
+    put(coals.data(), coals.size() * sizeof(uint32_t));
+    if (!g.miss_node.empty()) put(g.miss_node.data(), g.miss_node.size() * sizeof(uint32_t));
+    out.flush();
+    GRGX_CHECK(out.good(), GRGX_ERR_API_MISUSE, "Writing GRG failed");
 }
 
 void materialize_edges(HostGraph& g) {

@@ -61,6 +61,8 @@ void materialize_edges(HostGraph& g);
 
 // Load a .grg file (format 5.x, serialize.cpp:815-890 + readGrgCommon :697-758).
 std::unique_ptr<HostGraph> load_grg_file(const std::string& path);
+// Save a (decoded) graph as a .grg file (format 5.3) that load_grg_file reads back.
+void save_grg_file(const HostGraph& g, const std::string& path);
 
 // Seeded window-tree generator (one Kingman tree per 100-variant window, collapsed to its
 // mutation nodes).

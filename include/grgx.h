@@ -103,6 +103,12 @@ grgx_status grgx_graph_from_csr(uint64_t num_nodes, uint64_t num_samples, uint64
 grgx_status grgx_graph_generate(uint64_t num_samples, uint64_t num_mutations, uint64_t seed, uint32_t window,
                                 int threads, grgx_graph** out);
 
+/* Replaces grgl::saveGRG(grg, path, allowSimplify=false) (src/serialize.cpp:939-942, writer
+ * :517-669) for graphs whose children are ascending within each node: writes format 5.3, which
+ * grgx_graph_load reads back.  Mutations are written with REF "A" / ALT "C" and the stored
+ * positions (the matmul path reads neither). */
+grgx_status grgx_graph_save(const grgx_graph* g, const char* path);
+
 void grgx_graph_destroy(grgx_graph* g);
 
 grgx_status grgx_graph_info_get(const grgx_graph* g, grgx_graph_info* out);

@@ -171,3 +171,47 @@ def test_loader_keeps_buckets_encoded_until_needed(gx, tmp_path):
     assert gb is not None and gb.num_edges == o.num_edges
     with pytest.raises(RuntimeError, match="Malformed GRG file"):
         gb.export_arrays()
+
+
+def test_save_round_trip(gx, tmp_path):
+    """A saved graph reads back with the same arrays (and, where the reference build exists in
+    this checkout, the reference reads it to the same products as the oracle)."""
+    g = gx.window_tree_grg(600, 5000, seed=13)
+    path = tmp_path / "wt.grg"
+    g.save(str(path))
+    back = gx.load_immutable_grg(str(path))
+    a, b = g.export_arrays(), back.export_arrays()
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
+    o = oracle.read_grg(path)
+    assert np.array_equal(o.down_adj, a["down_adj"]) and np.array_equal(o.mut_node, a["mut_node"])
+    bad = gx.from_csr(num_samples=2, ploidy=2, down_off=np.array([0, 0, 0, 2], dtype=np.uint64),
+                      down_adj=np.array([1, 0], dtype=np.uint32), mut_node=np.array([2], dtype=np.uint32))
+    with pytest.raises(RuntimeError, match="ascending"):
+        bad.save(str(tmp_path / "bad.grg"))
+
+
+def test_saved_file_reads_in_the_reference(gx, tmp_path):
+    import os
+    import sys
+
+    ref = ROOT / "oracle" / "_ref"
+    src = os.environ.get("GRGL_REF", "/root/reference")
+    if not (ref.exists() and os.path.isdir(src)):
+        pytest.skip("reference build not present")
+    sys.path[:0] = [str(ref), src]
+    try:
+        pygrgl = pytest.importorskip("pygrgl")
+    finally:
+        del sys.path[:2]
+    g = gx.window_tree_grg(500, 3000, seed=5)
+    path = str(tmp_path / "wt.grg")
+    g.save(path)
+    r = pygrgl.load_immutable_grg(path)
+    a = g.export_arrays()
+    og = oracle.OracleGraph(num_samples=500, ploidy=2, down_off=a["down_off"], down_adj=a["down_adj"],
+                            mut_node=a["mut_node"])
+    rng = np.random.default_rng(0)
+    V, W = rng.standard_normal((3, 500)), rng.standard_normal((2, 3000))
+    assert np.array_equal(pygrgl.matmul(r, V, pygrgl.TraversalDirection.UP), oracle.matmul(og, V, UP))
+    assert np.array_equal(pygrgl.matmul(r, W, pygrgl.TraversalDirection.DOWN), oracle.matmul(og, W, DOWN))
