@@ -1,0 +1,298 @@
+// UP in split form: height-0 children in sample-blocked passes, the rest level by level.
+//
+// In a window-tree GRG most UP edges point at samples (height-0 nodes), and they do so from
+// every level: a mutation node's children are its nearest mutated descendants *and* the samples
+// no lower mutation covers.  While the warps sweep a level they therefore touch every sample
+// row at once, and once N x K x s outgrows L2 (1M samples x 256 columns x 4 bytes is 1 GB)
+// nearly every gather comes from HBM -- ncu counts a 12% L2 hit rate and 86% of HBM throughput
+// on such UP levels.  Since height-0 values are final before the sweep starts, their edges can
+// all be taken first, in passes over blocks of consecutive height-0 ids whose rows stay in L2:
+//   pass j    every UP node with children in block j adds those children's rows into its
+//             accumulator state (Op::A, so compensated sums stay compensated between passes)
+//   level h   every UP node of height h with children of height >= 1 adds those and writes its
+//             value from state + sum; the nodes of height h without such children are written
+//             from their state alone
+// The split copy is built once per graph on the device from the resident UP CSR (children are
+// ascending, so each row's height-0 children are a prefix and each block a sub-range of it: one
+// thread per row finds the boundaries by binary search), the host lays out rows and chunks from
+// the boundaries, and one warp per row copies every edge to its place.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <string>
+#include <vector>
+
+#include "device_plan.h"
+
+namespace grgx {
+
+namespace {
+
+#define BL_CUDA(call)                                                                                \
+    do {                                                                                            \
+        cudaError_t e__ = (call);                                                                   \
+        if (e__ != cudaSuccess)                                                                     \
+            throw Error(e__ == cudaErrorMemoryAllocation ? GRGX_ERR_OUT_OF_MEMORY : GRGX_ERR_CUDA,  \
+                        std::string(#call) + ": " + cudaGetErrorString(e__));                        \
+    } while (0)
+
+std::atomic<unsigned long long> g_threshold{64ull << 20};
+std::atomic<long long> g_block{32768};
+
+unsigned blocks_for(unsigned long long items, unsigned perBlock) {
+    unsigned long long b = (items + perBlock - 1) / perBlock;
+    if (b > 152ull * 64) b = 152ull * 64;
+    return static_cast<unsigned>(b < 1 ? 1 : b);
+}
+
+// Per UP row i: seg[i*(nb+1) + b] = index (within the row) of its first child with id >=
+// min(b * block, src0), for b = 0..nb; seg[i*(nb+1) + nb] is where the children of height >= 1
+// start.
+__global__ void segment_kernel(const uint32_t* __restrict__ adj, const long long* __restrict__ off, long long R,
+                               int nb, long long block, long long src0, uint32_t* __restrict__ seg) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < R; i += (long long)gridDim.x * blockDim.x) {
+        const long long b0 = off[i], deg = off[i + 1] - b0;
+        long long lo = 0;
+        for (int b = 0; b <= nb; b++) {
+            const long long key = (static_cast<long long>(b) * block < src0) ? static_cast<long long>(b) * block : src0;
+            long long l = lo, h = deg;
+            while (l < h) {
+                const long long m = (l + h) >> 1;
+                if (static_cast<long long>(adj[b0 + m] & 0x7fffffffu) < key) l = m + 1;
+                else h = m;
+            }
+            seg[i * (nb + 1) + b] = static_cast<uint32_t>(l);
+            lo = l;
+        }
+    }
+}
+
+// One warp per UP row: every edge to its block segment (height-0 child) or to the row's
+// internal run, HEAD_BIT on the first edge of each segment and run.
+__global__ void scatter_kernel(const uint32_t* __restrict__ adj, const long long* __restrict__ off, long long R,
+                               int nb, long long block, long long src0, const uint32_t* __restrict__ seg,
+                               const long long* __restrict__ dst0, const long long* __restrict__ dstI,
+                               uint32_t* __restrict__ out0, uint32_t* __restrict__ outI) {
+    const int lane = threadIdx.x & 31;
+    const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+    for (long long i = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < R; i += warps) {
+        const long long b0 = off[i], deg = off[i + 1] - b0;
+        const long long p = seg[i * (nb + 1) + nb];
+        for (long long k = lane; k < deg; k += 32) {
+            const uint32_t c = adj[b0 + k] & 0x7fffffffu;
+            if (k < p) {
+                const int b = static_cast<int>(c / block);
+                const long long rel = k - seg[i * (nb + 1) + b];
+                out0[dst0[i * nb + b] + rel] = c | (rel == 0 ? HEAD_BIT : 0u);
+            } else {
+                const long long rel = k - p;
+                outI[dstI[i] + rel] = c | (rel == 0 ? HEAD_BIT : 0u);
+            }
+        }
+    }
+}
+
+template <class Op>
+__global__ void state_finish_kernel(const typename Op::A* __restrict__ state, typename Op::S* __restrict__ vals,
+                                    const int* __restrict__ nodes, long long count, long long base, long long stride,
+                                    int rmw, const int* gate, int gateValue) {
+    if (gate != nullptr && *gate != gateValue) return;
+    const long long total = count * stride;
+    for (long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x; x < total;
+         x += (long long)gridDim.x * blockDim.x) {
+        const long long node = nodes[x / stride], col = x % stride;
+        typename Op::S* d = vals + node * stride + col;
+        const typename Op::A a = state[(node - base) * stride + col];
+        *d = rmw ? Op::finish_onto(*d, a) : Op::finish(a);
+    }
+}
+
+template <class Op>
+void finish_as(const void* state, void* vals, const int* nodes, long long count, long long base, long long stride,
+               int rmw, cudaStream_t s, const int* gate, int gateValue) {
+    const long long total = count * stride;
+    if (total <= 0) return;
+    state_finish_kernel<Op><<<blocks_for(static_cast<unsigned long long>(total), 256), 256, 0, s>>>(
+        static_cast<const typename Op::A*>(state), static_cast<typename Op::S*>(vals), nodes, count, base, stride,
+        rmw, gate, gateValue);
+}
+
+DevCSR upload_pull(DevicePlan& d, PullCSR& P, uint32_t* adj, long long E) {
+    auto up = [&](const auto& v) -> void* {
+        if (v.empty()) return nullptr;
+        void* p = nullptr;
+        BL_CUDA(cudaMalloc(&p, v.size() * sizeof(v[0])));
+        d.allocs.push_back(p);
+        d.bytes += v.size() * sizeof(v[0]);
+        BL_CUDA(cudaMemcpy(p, v.data(), v.size() * sizeof(v[0]), cudaMemcpyHostToDevice));
+        return p;
+    };
+    DevCSR r;
+    r.adj = adj;
+    r.rows = static_cast<int*>(up(P.rows));
+    r.chunks = static_cast<ChunkDev*>(up(P.chunks));
+    r.heavy = static_cast<HeavyDev*>(up(P.heavy));
+    r.lb = P.level_chunk_begin;
+    r.le = P.level_chunk_end;
+    for (size_t l = 0; l < P.level_chunk_begin.size(); l++) {
+        const Chunk& a = P.chunks[static_cast<size_t>(P.level_chunk_begin[l])];
+        const Chunk& c = P.chunks[static_cast<size_t>(P.level_chunk_end[l])];
+        r.level_rows.push_back(static_cast<long long>(c.r0) - a.r0);
+        r.level_edges.push_back(static_cast<long long>(c.e0 - a.e0));
+    }
+    r.n_heavy = static_cast<long long>(P.heavy.size());
+    r.n_pieces = P.num_pieces;
+    r.n_edges = E;
+    r.n_rows = static_cast<long long>(P.rows.size());
+    return r;
+}
+
+}  // namespace
+
+uint64_t blocked_threshold_bytes() { return g_threshold.load(); }
+long long blocked_block_size() { return g_block.load(); }
+
+void set_blocking(long long block, unsigned long long thresholdBytes) {
+    if (block > 0) g_block.store(block);
+    g_threshold.store(thresholdBytes);
+}
+
+void launch_state_finish(Kind kind, const void* state, void* vals, const int* nodes, long long count,
+                         long long stateBase, long long stride, int rmw, cudaStream_t s, const int* gate,
+                         int gateValue) {
+#define GRGX_FIN(OP) finish_as<OP>(state, vals, nodes, count, stateBase, stride, rmw, s, gate, gateValue)
+    switch (kind) {
+    case Kind::U32: GRGX_FIN(AddU32); break;
+    case Kind::XOR: GRGX_FIN(XorU32); break;
+    case Kind::U64: GRGX_FIN(AddU64); break;
+    case Kind::F64: GRGX_FIN(AddF64); break;
+    case Kind::F32C: GRGX_FIN(AddF32C); break;
+    case Kind::F32: GRGX_FIN(AddF32); break;
+    case Kind::F64S: GRGX_FIN(AddF64S); break;
+    }
+#undef GRGX_FIN
+}
+
+// Builds d.up0b / d.up_int / d.fin from the resident UP CSR (rows = nodes level_begin[1] .. n-1
+// in order, children ascending).
+void build_up_split(DevicePlan& d, const HostPlan& hp) {
+    const long long block = blocked_block_size();
+    if (hp.num_levels < 2) return;
+    const long long src0 = static_cast<long long>(hp.level_begin[1]);
+    const long long n = static_cast<long long>(hp.level_begin[hp.num_levels]);
+    const long long R = n - src0;
+    const int nb = static_cast<int>((src0 + block - 1) / block);
+    if (nb < 2 || R == 0) return;
+    const std::vector<int64_t>& off = hp.up.off;
+    const long long E = off[R];
+    std::vector<void*> tmp;
+    auto dmalloc = [&](size_t bytes) {
+        void* p = nullptr;
+        BL_CUDA(cudaMalloc(&p, bytes ? bytes : 1));
+        tmp.push_back(p);
+        return p;
+    };
+    auto freeTmp = [&] {
+        for (void* p : tmp) cudaFree(p);
+        tmp.clear();
+    };
+    uint32_t *out0 = nullptr, *outI = nullptr;
+    try {
+        long long* dOff = static_cast<long long*>(dmalloc((R + 1) * sizeof(long long)));
+        BL_CUDA(cudaMemcpy(dOff, off.data(), (R + 1) * sizeof(long long), cudaMemcpyHostToDevice));
+        const size_t segN = static_cast<size_t>(R) * (nb + 1);
+        uint32_t* dSeg = static_cast<uint32_t*>(dmalloc(segN * sizeof(uint32_t)));
+        segment_kernel<<<blocks_for(R, 256), 256>>>(d.up.adj, dOff, R, nb, block, src0, dSeg);
+        BL_CUDA(cudaGetLastError());
+        std::vector<uint32_t> seg(segN);
+        BL_CUDA(cudaMemcpy(seg.data(), dSeg, segN * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+        auto S = [&](long long i, int b) { return static_cast<long long>(seg[static_cast<size_t>(i) * (nb + 1) + b]); };
+
+        // height-0 passes: block-major rows
+        PullCSR P0;
+        std::vector<int64_t> off0(1, 0), rowBegin0;
+        std::vector<long long> dst0(static_cast<size_t>(R) * nb, 0);
+        for (int b = 0; b < nb; b++) {
+            rowBegin0.push_back(static_cast<int64_t>(P0.rows.size()));
+            for (long long i = 0; i < R; i++) {
+                const long long len = S(i, b + 1) - S(i, b);
+                if (len <= 0) continue;
+                dst0[static_cast<size_t>(i) * nb + b] = off0.back();
+                P0.rows.push_back(static_cast<int32_t>(src0 + i));
+                off0.push_back(off0.back() + len);
+            }
+        }
+        rowBegin0.push_back(static_cast<int64_t>(P0.rows.size()));
+        for (int b = 0; b < nb; b++) chunk_level(P0, off0, rowBegin0[b], rowBegin0[b + 1]);
+        finish_csr(P0, off0);
+        const long long E0 = off0.back();
+
+        // internal edges: one level per UP level (heights 1..H-1), plus the finish lists
+        PullCSR PI;
+        std::vector<int64_t> offI(1, 0), rowBeginI;
+        std::vector<long long> dstI(static_cast<size_t>(R), -1);
+        std::vector<int> fin;
+        std::vector<long long> finBegin;
+        for (uint64_t h = 1; h < hp.num_levels; h++) {
+            rowBeginI.push_back(static_cast<int64_t>(PI.rows.size()));
+            finBegin.push_back(static_cast<long long>(fin.size()));
+            for (long long node = static_cast<long long>(hp.level_begin[h]);
+                 node < static_cast<long long>(hp.level_begin[h + 1]); node++) {
+                const long long i = node - src0;
+                const long long len = (off[i + 1] - off[i]) - S(i, nb);
+                if (len <= 0) {
+                    fin.push_back(static_cast<int>(node));
+                    continue;
+                }
+                dstI[static_cast<size_t>(i)] = offI.back();
+                PI.rows.push_back(static_cast<int32_t>(node));
+                offI.push_back(offI.back() + len);
+            }
+        }
+        rowBeginI.push_back(static_cast<int64_t>(PI.rows.size()));
+        finBegin.push_back(static_cast<long long>(fin.size()));
+        for (size_t h = 0; h + 1 < rowBeginI.size(); h++) chunk_level(PI, offI, rowBeginI[h], rowBeginI[h + 1]);
+        finish_csr(PI, offI);
+        const long long EI = offI.back();
+        GRGX_CHECK(E0 + EI == E, GRGX_ERR_CUDA, "split edge count mismatch");
+
+        long long* dDst0 = static_cast<long long*>(dmalloc(dst0.size() * sizeof(long long)));
+        long long* dDstI = static_cast<long long*>(dmalloc(dstI.size() * sizeof(long long)));
+        BL_CUDA(cudaMemcpy(dDst0, dst0.data(), dst0.size() * sizeof(long long), cudaMemcpyHostToDevice));
+        BL_CUDA(cudaMemcpy(dDstI, dstI.data(), dstI.size() * sizeof(long long), cudaMemcpyHostToDevice));
+        BL_CUDA(cudaMalloc(reinterpret_cast<void**>(&out0), (E0 ? E0 : 1) * sizeof(uint32_t)));
+        BL_CUDA(cudaMalloc(reinterpret_cast<void**>(&outI), (EI ? EI : 1) * sizeof(uint32_t)));
+        scatter_kernel<<<blocks_for(R, 8), 256>>>(d.up.adj, dOff, R, nb, block, src0, dSeg, dDst0, dDstI, out0, outI);
+        BL_CUDA(cudaGetLastError());
+        BL_CUDA(cudaDeviceSynchronize());
+        freeTmp();
+        uint32_t* a0 = out0;
+        uint32_t* aI = outI;
+        d.allocs.push_back(a0);
+        out0 = nullptr;
+        d.allocs.push_back(aI);
+        outI = nullptr;
+        d.bytes += static_cast<uint64_t>(E0 + EI) * sizeof(uint32_t);
+        d.up0b = upload_pull(d, P0, a0, E0);
+        d.up_int = upload_pull(d, PI, aI, EI);
+        if (!fin.empty()) {
+            void* p = nullptr;
+            BL_CUDA(cudaMalloc(&p, fin.size() * sizeof(int)));
+            d.allocs.push_back(p);
+            d.bytes += fin.size() * sizeof(int);
+            BL_CUDA(cudaMemcpy(p, fin.data(), fin.size() * sizeof(int), cudaMemcpyHostToDevice));
+            d.fin = static_cast<int*>(p);
+        }
+        d.fin_begin = finBegin;
+        d.split_block = block;
+        d.split_src = src0;
+    } catch (...) {
+        freeTmp();
+        if (out0) cudaFree(out0);
+        if (outI) cudaFree(outI);
+        throw;
+    }
+}
+
+}  // namespace grgx

@@ -33,6 +33,16 @@ struct DevCSR {
 struct DevicePlan {
     int device = -1;
     DevCSR up, down, seed, miss;
+    // UP in split form (empty when the height-0 nodes make fewer than two blocks):
+    //   up0b    the edges to height-0 children, cut by blocks of `split_block` height-0 ids;
+    //           level j = block j, rows = every node with children in the block
+    //   up_int  the edges to children of height >= 1, one level per UP level (same order)
+    //   fin     per UP level, the nodes without such children (finished from their state alone),
+    //           concatenated; fin_begin[j] .. fin_begin[j+1] for level j
+    DevCSR up0b, up_int;
+    int* fin = nullptr;
+    std::vector<long long> fin_begin;
+    long long split_block = 0, split_src = 0;  // split_src = height-0 ids = first UP row's node id
     uint32_t* mut_new = nullptr;
     uint32_t* miss_new = nullptr;
     uint32_t* old2new = nullptr;
@@ -79,9 +89,23 @@ int sm_count();
 // Launches one level of a CSR (a no-op when the level has no chunks); `work` points at
 // `tileStride` (0: L.ntiles) zeroed counters owned by this launch, and the heavy-row tickets
 // are `tileStride` apart.  `shape` null: the default shape.  Returns the kernels launched.
+// `state` set: each node's Op::A accumulator lives at state + (node - stateBase) rows; with
+// stateMode 1 a row's sum is merged into it (nothing written), with 2 the node value is written
+// from the accumulator merged with the row's sum.
 int launch_level(const Layout& L, const DevCSR& c, size_t level, const void* src, void* dst, int rmw,
                  void* partials, unsigned* tickets, unsigned* work, cudaStream_t s, const int* gate = nullptr,
-                 int gateValue = 0, const LevelShape* shape = nullptr, int tileStride = 0);
+                 int gateValue = 0, const LevelShape* shape = nullptr, int tileStride = 0, void* state = nullptr,
+                 long long stateBase = 0, int stateMode = 1);
+
+// UP in split form (blocked.cu): writes vals[node] from its accumulator state (added onto the
+// value when rmw) for the `count` nodes listed at `nodes`.
+void launch_state_finish(Kind kind, const void* state, void* vals, const int* nodes, long long count,
+                         long long stateBase, long long stride, int rmw, cudaStream_t s, const int* gate,
+                         int gateValue);
+// Height-0 row bytes (height-0 ids x stride x element size) above which UP runs in split form,
+// and the block of height-0 ids each split pass covers; both adjustable for tests.
+uint64_t blocked_threshold_bytes();
+long long blocked_block_size();
 
 // Builds (once) and returns the graph's plan on the current device.
 DevicePlan* ensure_device_plan(grgx_graph* g);

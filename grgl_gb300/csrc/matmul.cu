@@ -172,6 +172,9 @@ SweepParams<S> make_params(const DevCSR& c, long long cb, long long ce, const vo
     p.ntiles = ntiles;
     p.gate = nullptr;
     p.gate_value = 0;
+    p.state = nullptr;
+    p.state_base = 0;
+    p.state_mode = 0;
     return p;
 }
 
@@ -179,7 +182,8 @@ SweepParams<S> make_params(const DevCSR& c, long long cb, long long ce, const vo
 // `work` points at L.ntiles zeroed counters owned by this launch.
 int launch_level(const Layout& L, const DevCSR& c, size_t level, const void* src, void* dst, int rmw,
                  void* partials, unsigned* tickets, unsigned* work, cudaStream_t s, const int* gate,
-                 int gateValue, const LevelShape* shape, int tileStride) {
+                 int gateValue, const LevelShape* shape, int tileStride, void* state, long long stateBase,
+                 int stateMode) {
     const long long cb = c.lb[level], ce = c.le[level];
     if (ce <= cb) return 0;
     const LevelShape sh = shape ? *shape : default_shape(L);
@@ -192,6 +196,9 @@ int launch_level(const Layout& L, const DevCSR& c, size_t level, const void* src
         SweepParams<S> p = make_params<S>(c, cb, ce, src, dst, L.stride, rmw, partials, tickets, work, ts);
         p.gate = gate;
         p.gate_value = gateValue;
+        p.state = state;
+        p.state_base = stateBase;
+        p.state_mode = stateMode;
         return p;
     };
     const int vw = L.vw, g = sh.g, v = sh.variant;
@@ -227,6 +234,7 @@ uint32_t* build_plan_device(const HostGraph& g, const unsigned long long* dOff, 
                             HostPlan& plan);
 
 void decode_edges_device(const HostGraph& hg, void** dOff, void** dAdj);
+void build_up_split(DevicePlan& d, const HostPlan& hp);
 
 namespace {
 // The E-sized passes of the plan on the device (plan_device.cu) from the down CSR, uploaded
@@ -304,6 +312,7 @@ DevicePlan* ensure_device_plan(grgx_graph* g) {
     d->has_miss = hp.has_miss;
     for (uint32_t x : hp.xtx_new)
         if (x != COAL_NOT_SET) d->xtx_max = std::max(d->xtx_max, static_cast<double>(x));
+    build_up_split(*d, hp);
     g->dev = std::move(d);
     g->plan.reset();  // the device copy is authoritative; free the host copy
     return g->dev.get();
@@ -417,12 +426,21 @@ void matmul_direct(grgx_graph* g, int dtype, const void* input, uint64_t in_cols
         // ---- node values and the per-call scratch ---------------------------------------------
         const size_t valBytes = static_cast<size_t>(n) * L.stride * L.ssize;
         void* vals = sc.get(valBytes);
+        // UP in split form when the height-0 rows outgrow L2: their edges first, in blocked
+        // passes, then the other edges level by level (blocked.cu)
+        const bool split = !down && dp->up0b.n_rows > 0 &&
+                           static_cast<uint64_t>(dp->split_src) * static_cast<uint64_t>(L.stride) * L.ssize >
+                               blocked_threshold_bytes();
         long long pieces = down ? std::max(dp->down.n_pieces, std::max(dp->seed.n_pieces, dp->miss.n_pieces))
-                                : dp->up.n_pieces;
+                                : (split ? std::max(dp->up0b.n_pieces, dp->up_int.n_pieces) : dp->up.n_pieces);
         void* partials = sc.get(static_cast<size_t>(pieces) * L.stride * L.asize);
-        const long long nh = down ? (dp->down.n_heavy + dp->seed.n_heavy + dp->miss.n_heavy) : dp->up.n_heavy;
+        const long long nh = down ? (dp->down.n_heavy + dp->seed.n_heavy + dp->miss.n_heavy)
+                                  : (split ? dp->up0b.n_heavy + dp->up_int.n_heavy : dp->up.n_heavy);
         const long long nslots = down ? (2 + static_cast<long long>(dp->down.lb.size()))
-                                      : static_cast<long long>(dp->up.lb.size());
+                                      : static_cast<long long>(split ? dp->up0b.lb.size() + dp->up_int.lb.size()
+                                                                     : dp->up.lb.size());
+        const size_t stateBytes = split ? static_cast<size_t>(n - dp->split_src) * L.stride * std::max(L.asize, 8) : 0;
+        void* state = split ? sc.get(stateBytes) : nullptr;
         // counters per launch and per heavy row: enough column tiles for any launch shape
         const int TS = max_tiles(L);
         const size_t counterBytes = static_cast<size_t>(nh + nslots) * TS * sizeof(unsigned);
@@ -541,8 +559,33 @@ void matmul_direct(grgx_graph* g, int dtype, const void* input, uint64_t in_cols
                 // UP seed: samples <- input columns
                 load_rows(dIn, in_cols, N, by_indiv ? MAP_DIV : MAP_IDENT, P, nullptr, vals, hasInit);
                 if (timed && t_timing) GRGX_CUDA(cudaEventRecord(ev[1], s));
-                for (size_t lvl = 0; lvl < dp->up.lb.size(); lvl++)
-                    launches += level(dp->up, lvl, vals, hasInit, tickets, work + lvl * TS);
+                if (split) {
+                    GRGX_CUDA(cudaMemsetAsync(state, 0, stateBytes, s));
+                    unsigned* t0b = tickets;
+                    unsigned* tIn = tickets + dp->up0b.n_heavy * TS;
+                    unsigned* w0b = work;
+                    unsigned* wIn = work + dp->up0b.lb.size() * TS;
+                    const long long base = dp->split_src;
+                    for (size_t j = 0; j < dp->up0b.lb.size(); j++) {
+                        const LevelShape sh = level_shape(LL, dp->up0b, j);
+                        launches += launch_level(LL, dp->up0b, j, vals, vals, 0, partials, t0b, w0b + j * TS, s, g,
+                                                 gv, &sh, TS, state, base, 1);
+                    }
+                    for (size_t lvl = 0; lvl < dp->up_int.lb.size(); lvl++) {
+                        const LevelShape sh = level_shape(LL, dp->up_int, lvl);
+                        launches += launch_level(LL, dp->up_int, lvl, vals, vals, hasInit, partials, tIn,
+                                                 wIn + lvl * TS, s, g, gv, &sh, TS, state, base, 2);
+                        const long long f0 = dp->fin_begin[lvl], f1 = dp->fin_begin[lvl + 1];
+                        if (f1 > f0) {
+                            launch_state_finish(LL.kind, state, vals, dp->fin + f0, f1 - f0, base, LL.stride, hasInit,
+                                                s, g, gv);
+                            launches++;
+                        }
+                    }
+                } else {
+                    for (size_t lvl = 0; lvl < dp->up.lb.size(); lvl++)
+                        launches += level(dp->up, lvl, vals, hasInit, tickets, work + lvl * TS);
+                }
                 if (timed && t_timing) GRGX_CUDA(cudaEventRecord(ev[2], s));
                 if (emit_all) {
                     store_cols(n, MAP_TABLE, 1, dp->old2new, dOut, out_cols, add);

@@ -49,6 +49,9 @@ template <typename S> struct SweepParams {
     int ntiles;
     const int* gate;           // when set, the launch runs only if *gate == gate_value
     int gate_value;
+    void* state;               // per-node Op::A carried between launches (UP split passes), or null
+    long long state_base;      // node id of the first state row
+    int state_mode;            // 1: merge each row sum into its state; 2: write state + row sum
 };
 
 template <typename S, int VW> struct Vec;
@@ -80,25 +83,6 @@ template <class Op, int VW, int G> __device__ __forceinline__ void group_allredu
     }
 }
 
-template <class Op, int VW>
-__device__ __forceinline__ void write_row(const SweepParams<typename Op::S>& p, long long row, int col,
-                                          const VecAcc<Op, VW>& tot) {
-    using S = typename Op::S;
-    const long long node = p.rows[row];
-    S* d = p.dst + node * p.stride + col;
-    S out[VW];
-    if (p.rmw) {
-        S base[VW];
-        ld_plain<S, VW>(d, base);
-#pragma unroll
-        for (int i = 0; i < VW; i++) out[i] = Op::finish_onto(base[i], tot.get(i));
-    } else {
-#pragma unroll
-        for (int i = 0; i < VW; i++) out[i] = Op::finish(tot.get(i));
-    }
-    Vec<S, VW>::st(d, out);
-}
-
 // L2-coherent loads for the heavy-row partials written by other warps of the same launch.
 __device__ __forceinline__ uint32_t ld_cg(const uint32_t* p) { return __ldcg(p); }
 __device__ __forceinline__ unsigned long long ld_cg(const unsigned long long* p) { return __ldcg(p); }
@@ -113,6 +97,45 @@ __device__ __forceinline__ F64Run ld_cg(const F64Run* p) {
 __device__ __forceinline__ F32Pair ld_cg(const F32Pair* p) {
     const float2 t = __ldcg(reinterpret_cast<const float2*>(p));
     return {t.x, t.y};
+}
+
+template <class Op, int VW>
+__device__ __forceinline__ void write_row(const SweepParams<typename Op::S>& p, long long row, int col,
+                                          const VecAcc<Op, VW>& tot) {
+    using S = typename Op::S;
+    using A = typename Op::A;
+    const long long node = p.rows[row];
+    A sum[VW];
+#pragma unroll
+    for (int i = 0; i < VW; i++) sum[i] = tot.get(i);
+    if (p.state != nullptr) {
+        // the node's sum so far (earlier passes) stays in accumulator form: merge into it, and
+        // either keep it (mode 1) or write the node value from it (mode 2)
+        A* st = static_cast<A*>(p.state) + (node - p.state_base) * p.stride + col;
+#pragma unroll
+        for (int i = 0; i < VW; i++) {
+            A cur = ld_cg(st + i);
+            Op::merge(cur, sum[i]);
+            sum[i] = cur;
+        }
+        if (p.state_mode == 1) {
+#pragma unroll
+            for (int i = 0; i < VW; i++) st[i] = sum[i];
+            return;
+        }
+    }
+    S* d = p.dst + node * p.stride + col;
+    S out[VW];
+    if (p.rmw) {
+        S base[VW];
+        ld_plain<S, VW>(d, base);
+#pragma unroll
+        for (int i = 0; i < VW; i++) out[i] = Op::finish_onto(base[i], sum[i]);
+    } else {
+#pragma unroll
+        for (int i = 0; i < VW; i++) out[i] = Op::finish(sum[i]);
+    }
+    Vec<S, VW>::st(d, out);
 }
 
 // Accumulators may bound their running chains: AddF64S renormalises its float pair every 4
