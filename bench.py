@@ -483,7 +483,7 @@ def main():
         t0 = time.perf_counter()
         levels_tuned = 0
         for dt, K, d in dict.fromkeys(combos):
-            levels_tuned += gx.autotune(g, dt, K, d).count("level ")
+            levels_tuned += sum(1 for ln in gx.autotune(g, dt, K, d).splitlines() if " rows " in ln)
         torch.cuda.synchronize()
         table = gx.autotune_table()
         tune = {"seconds": time.perf_counter() - t0, "levels_tuned": levels_tuned,

@@ -143,18 +143,41 @@ std::string autotune_impl(grgx_graph* g, int dtype, uint64_t rows, int direction
     const Layout L = choose_layout(dtype, static_cast<long long>(rows), (flags & GRGX_FLAG_F32_PLAIN) != 0,
                                    (flags & GRGX_FLAG_F64_NATIVE) != 0);
     const bool down = (direction == GRGX_DIRECTION_DOWN);
-    const DevCSR& c = down ? dp->down : dp->up;
+    // the CSRs a call of this shape sweeps: UP in split form (blocked.cu) when it would run so
+    struct Pass {
+        const DevCSR* c;
+        int mode;
+        const char* name;
+    };
+    std::vector<Pass> passes;
+    const bool split = !down && dp->up0b.n_rows > 0 &&
+                       static_cast<uint64_t>(dp->split_src) * static_cast<uint64_t>(L.stride) * L.ssize >
+                           blocked_threshold_bytes();
+    if (down) passes.push_back({&dp->down, 0, "level"});
+    else if (split) {
+        passes.push_back({&dp->up0b, 1, "height-0 block"});
+        passes.push_back({&dp->up_int, 2, "level"});
+    } else {
+        passes.push_back({&dp->up, 0, "level"});
+    }
+    long long maxPieces = 0, maxHeavy = 0, totalEdges = 0;
+    for (const Pass& ps : passes) {
+        maxPieces = std::max(maxPieces, ps.c->n_pieces);
+        maxHeavy = std::max(maxHeavy, ps.c->n_heavy);
+        totalEdges += ps.c->n_edges;
+    }
     const int maxT = max_tiles(L);
     const size_t n = g->host->num_nodes;
     cudaStream_t s = nullptr;
     GRGX_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
-    void *vals = nullptr, *partials = nullptr;
+    void *vals = nullptr, *partials = nullptr, *state = nullptr;
     unsigned* counters = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     std::ostringstream rep;
     auto release = [&] {
         if (vals) cudaFree(vals);
         if (partials) cudaFree(partials);
+        if (state) cudaFree(state);
         if (counters) cudaFree(counters);
         if (e0) cudaEventDestroy(e0);
         if (e1) cudaEventDestroy(e1);
@@ -164,20 +187,28 @@ std::string autotune_impl(grgx_graph* g, int dtype, uint64_t rows, int direction
         const size_t valBytes = n * static_cast<size_t>(L.stride) * L.ssize;
         GRGX_CUDA(cudaMalloc(&vals, std::max<size_t>(valBytes, 16)));
         GRGX_CUDA(cudaMemsetAsync(vals, 0, valBytes, s));
-        GRGX_CUDA(cudaMalloc(&partials, std::max<size_t>(static_cast<size_t>(c.n_pieces) * L.stride * L.asize, 16)));
-        const size_t counterBytes = static_cast<size_t>(c.n_heavy + 1) * maxT * sizeof(unsigned);
+        GRGX_CUDA(cudaMalloc(&partials, std::max<size_t>(static_cast<size_t>(maxPieces) * L.stride * L.asize, 16)));
+        if (split) {
+            const size_t stateBytes = (n - static_cast<size_t>(dp->split_src)) * L.stride * std::max(L.asize, 8);
+            GRGX_CUDA(cudaMalloc(&state, std::max<size_t>(stateBytes, 16)));
+            GRGX_CUDA(cudaMemsetAsync(state, 0, stateBytes, s));
+        }
+        const size_t counterBytes = static_cast<size_t>(maxHeavy + 1) * maxT * sizeof(unsigned);
         GRGX_CUDA(cudaMalloc(&counters, counterBytes));
         GRGX_CUDA(cudaEventCreate(&e0));
         GRGX_CUDA(cudaEventCreate(&e1));
         unsigned* tickets = counters;
-        unsigned* work = counters + c.n_heavy * maxT;
+        unsigned* work = counters + maxHeavy * maxT;
         const int rmw = down ? 1 : 0;
+        const DevCSR* cur = nullptr;
+        int curMode = 0;
         auto time_shape = [&](size_t lvl, const LevelShape& sh) {
             float best = 1e30f;
             for (int rep_i = 0; rep_i < 3; rep_i++) {
                 GRGX_CUDA(cudaMemsetAsync(counters, 0, counterBytes, s));
                 GRGX_CUDA(cudaEventRecord(e0, s));
-                launch_level(L, c, lvl, vals, vals, rmw, partials, tickets, work, s, nullptr, 0, &sh, maxT);
+                launch_level(L, *cur, lvl, vals, vals, rmw, partials, tickets, work, s, nullptr, 0, &sh, maxT,
+                             curMode ? state : nullptr, dp->split_src, curMode ? curMode : 1);
                 GRGX_CUDA(cudaEventRecord(e1, s));
                 GRGX_CUDA(cudaEventSynchronize(e1));
                 GRGX_CUDA(cudaGetLastError());
@@ -189,10 +220,14 @@ std::string autotune_impl(grgx_graph* g, int dtype, uint64_t rows, int direction
         };
         const std::vector<int> gs = candidate_g(L);
         double totDefault = 0, totBest = 0;
+        for (const Pass& ps : passes) {
+        cur = ps.c;
+        curMode = ps.mode;
+        const DevCSR& c = *ps.c;
         for (size_t lvl = 0; lvl < c.lb.size(); lvl++) {
             if (c.le[lvl] <= c.lb[lvl]) continue;
             // levels under 0.5% of the traversal's edges keep the default untimed
-            if (c.level_edges[lvl] * 200 < c.n_edges) continue;
+            if (c.level_edges[lvl] * 200 < totalEdges) continue;
             const LevelShape def = default_shape(L);
             const float tDef = time_shape(lvl, def);
             LevelShape best = def;
@@ -223,11 +258,12 @@ std::string autotune_impl(grgx_graph* g, int dtype, uint64_t rows, int direction
             }
             char line[256];
             std::snprintf(line, sizeof(line),
-                          "level %zu rows %lld edges %lld: g %d tiles %d variant %d, %.4f ms (default g %d variant "
+                          "%s %zu rows %lld edges %lld: g %d tiles %d variant %d, %.4f ms (default g %d variant "
                           "0: %.4f ms)\n",
-                          lvl, c.level_rows[lvl], c.level_edges[lvl], best.g, best.ntiles, best.variant, tBest,
-                          def.g, tDef);
+                          ps.name, lvl, c.level_rows[lvl], c.level_edges[lvl], best.g, best.ntiles, best.variant,
+                          tBest, def.g, tDef);
             rep << line;
+        }
         }
         char tail[160];
         std::snprintf(tail, sizeof(tail), "sweep %.4f ms tuned, %.4f ms default\n", totBest, totDefault);
