@@ -81,6 +81,12 @@ def workload(args):
     return [(dt, K, d) for dt in dts for K in ks for d in (UP, DOWN)]
 
 
+def workload_name(args, combos):
+    return (f"plain matmul, window-tree GRG N={args.samples} M={args.mutations} seed={args.seed}, "
+            + (f"K in {{{args.ks}}}, UP+DOWN, {args.dtypes}" if not args.only else args.only)
+            + f"; {len(combos)} matmuls per step")
+
+
 def make_inputs(rng, combos, N, M):
     out = []
     for dt, K, d in combos:
@@ -411,8 +417,7 @@ def run_reference(args):
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "int32,float32,float64", "data": "synthetic (seeded window-tree GRG)", "impl": "reference",
-            "config": {"workload": f"plain matmul, window-tree GRG N={args.samples} M={args.mutations}, "
-                                   f"K in {{{args.ks}}}, UP+DOWN, {args.dtypes}"},
+            "config": {"workload": workload_name(args, combos)},
             "cpu_baseline": dict(cb, value=v),
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -608,9 +613,7 @@ def main():
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "int32,float32,float64", "data": "synthetic (seeded window-tree GRG)",
-            "config": {"workload": f"plain matmul, window-tree GRG N={args.samples} M={args.mutations} seed={args.seed}, "
-                                   + (f"K in {{{args.ks}}}, UP+DOWN, {args.dtypes}" if not args.only else args.only)
-                                   + f"; {len(combos)} matmuls per step",
+            "config": {"workload": workload_name(args, combos),
                        "graph": stats, "l2": "inputs larger than L2 (edge CSR streamed every traversal)",
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
