@@ -541,8 +541,8 @@ def matmul_batch(grg: GRG, requests, max_cols: int = 0, *, f32_compensated: bool
     ``requests`` is a list of ``(input, direction)`` or ``(input, direction, standardized)``;
     inputs are all numpy arrays or all CUDA tensors.  A standardized request computes what
     ``matmul_standardized`` does.  Returns the outputs in order.  Requests of the same direction
-    and dtype are stacked into traversals of at most ``max_cols`` rows (0 = the sweep's natural
-    width).
+    and dtype are stacked into traversals of at most ``max_cols`` rows (0 = 512 for 4-byte and
+    smaller dtypes, 256 for 8-byte ones).
     """
     prepared = [_request_for(grg, r[0], r[1], bool(r[2]) if len(r) > 2 else False) for r in requests]
     if not prepared:

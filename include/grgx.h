@@ -193,8 +193,8 @@ typedef struct {
 
 /* No counterpart in the reference (its callers loop over matMul calls).  Runs `n` requests on
  * one graph with as few traversals as possible: requests of the same direction and dtype are
- * stacked row-wise into traversals of at most `max_cols` columns (0 = a default sized for the
- * sweep's vector width), so the edge stream and the launches are shared.  Each request's
+ * stacked row-wise into traversals of at most `max_cols` columns (0 = 512 four-byte or 256
+ * eight-byte columns), so the edge stream and the launches are shared.  Each request's
  * result equals its own grgx_matmul result (bit-exact for integers; float sums may round
  * differently because the stacked row is wider).  Flags as grgx_matmul
  * (GRGX_FLAG_DEVICE_POINTERS, GRGX_FLAG_F32_PLAIN, GRGX_FLAG_F64_NATIVE). */
