@@ -324,11 +324,11 @@ def cold_start(gx, torch, g):
         g2.upload()
         torch.cuda.synchronize()
         t_up = time.perf_counter() - t0
-        same = g2.info()["device_bytes"] == g.info()["device_bytes"]
+        resident = g2.info()["device_bytes"]
         del g2
         torch.cuda.empty_cache()
         return {"file_bytes": size, "edges": g.num_edges, "save_s": t_save, "read_s": t_load,
-                "decode_and_plan_on_gpu_s": t_up, "load_to_resident_s": t_load + t_up, "same_plan_size": same}
+                "decode_and_plan_on_gpu_s": t_up, "load_to_resident_s": t_load + t_up, "device_bytes": resident}
     except (OSError, RuntimeError) as e:
         return {"unavailable": str(e)}
     finally:

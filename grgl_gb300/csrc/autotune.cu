@@ -150,9 +150,7 @@ std::string autotune_impl(grgx_graph* g, int dtype, uint64_t rows, int direction
         const char* name;
     };
     std::vector<Pass> passes;
-    const bool split = !down && dp->up0b.n_rows > 0 &&
-                       static_cast<uint64_t>(dp->split_src) * static_cast<uint64_t>(L.stride) * L.ssize >
-                           blocked_threshold_bytes();
+    const bool split = !down && use_up_split(g, dp, L);
     if (down) passes.push_back({&dp->down, 0, "level"});
     else if (split) {
         passes.push_back({&dp->up0b, 1, "height-0 block"});

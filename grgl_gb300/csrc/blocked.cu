@@ -20,6 +20,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -174,17 +175,17 @@ void launch_state_finish(Kind kind, const void* state, void* vals, const int* no
 #undef GRGX_FIN
 }
 
+namespace {
 // Builds d.up0b / d.up_int / d.fin from the resident UP CSR (rows = nodes level_begin[1] .. n-1
 // in order, children ascending).
-void build_up_split(DevicePlan& d, const HostPlan& hp) {
+void build_up_split(DevicePlan& d) {
     const long long block = blocked_block_size();
-    if (hp.num_levels < 2) return;
-    const long long src0 = static_cast<long long>(hp.level_begin[1]);
-    const long long n = static_cast<long long>(hp.level_begin[hp.num_levels]);
+    const long long src0 = static_cast<long long>(d.level_begin[1]);
+    const long long n = static_cast<long long>(d.level_begin[d.num_levels]);
     const long long R = n - src0;
     const int nb = static_cast<int>((src0 + block - 1) / block);
     if (nb < 2 || R == 0) return;
-    const std::vector<int64_t>& off = hp.up.off;
+    const std::vector<int64_t>& off = d.up_off;
     const long long E = off[R];
     std::vector<void*> tmp;
     auto dmalloc = [&](size_t bytes) {
@@ -234,11 +235,11 @@ void build_up_split(DevicePlan& d, const HostPlan& hp) {
         std::vector<long long> dstI(static_cast<size_t>(R), -1);
         std::vector<int> fin;
         std::vector<long long> finBegin;
-        for (uint64_t h = 1; h < hp.num_levels; h++) {
+        for (uint64_t h = 1; h < d.num_levels; h++) {
             rowBeginI.push_back(static_cast<int64_t>(PI.rows.size()));
             finBegin.push_back(static_cast<long long>(fin.size()));
-            for (long long node = static_cast<long long>(hp.level_begin[h]);
-                 node < static_cast<long long>(hp.level_begin[h + 1]); node++) {
+            for (long long node = static_cast<long long>(d.level_begin[h]);
+                 node < static_cast<long long>(d.level_begin[h + 1]); node++) {
                 const long long i = node - src0;
                 const long long len = (off[i + 1] - off[i]) - S(i, nb);
                 if (len <= 0) {
@@ -293,6 +294,22 @@ void build_up_split(DevicePlan& d, const HostPlan& hp) {
         if (outI) cudaFree(outI);
         throw;
     }
+}
+}  // namespace
+
+bool use_up_split(grgx_graph* g, DevicePlan* dp, const Layout& L) {
+    if (dp->num_levels < 2 || dp->level_begin.size() < 2) return false;
+    const long long src0 = static_cast<long long>(dp->level_begin[1]);
+    if (static_cast<uint64_t>(src0) * static_cast<uint64_t>(L.stride) * L.ssize <= blocked_threshold_bytes())
+        return false;
+    {
+        std::lock_guard<std::mutex> lk(g->mu);
+        if (!dp->split_built) {
+            build_up_split(*dp);
+            dp->split_built = true;
+        }
+    }
+    return dp->up0b.n_rows > 0;
 }
 
 }  // namespace grgx

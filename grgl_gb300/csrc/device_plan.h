@@ -39,10 +39,15 @@ struct DevicePlan {
     //   up_int  the edges to children of height >= 1, one level per UP level (same order)
     //   fin     per UP level, the nodes without such children (finished from their state alone),
     //           concatenated; fin_begin[j] .. fin_begin[j+1] for level j
+    // Built on the first call that runs UP in split form (use_up_split), from the UP row offsets
+    // and level boundaries kept here.
     DevCSR up0b, up_int;
     int* fin = nullptr;
     std::vector<long long> fin_begin;
     long long split_block = 0, split_src = 0;  // split_src = height-0 ids = first UP row's node id
+    bool split_built = false;
+    std::vector<int64_t> up_off;         // UP row offsets (host copy)
+    std::vector<uint64_t> level_begin;   // node-id range of each height
     uint32_t* mut_new = nullptr;
     uint32_t* miss_new = nullptr;
     uint32_t* old2new = nullptr;
@@ -106,6 +111,8 @@ void launch_state_finish(Kind kind, const void* state, void* vals, const int* no
 // and the block of height-0 ids each split pass covers; both adjustable for tests.
 uint64_t blocked_threshold_bytes();
 long long blocked_block_size();
+// Whether a call with layout L runs UP in split form; builds the split copy on first use.
+bool use_up_split(grgx_graph* g, DevicePlan* dp, const Layout& L);
 
 // Builds (once) and returns the graph's plan on the current device.
 DevicePlan* ensure_device_plan(grgx_graph* g);

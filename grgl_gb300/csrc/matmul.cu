@@ -234,7 +234,6 @@ uint32_t* build_plan_device(const HostGraph& g, const unsigned long long* dOff, 
                             HostPlan& plan);
 
 void decode_edges_device(const HostGraph& hg, void** dOff, void** dAdj);
-void build_up_split(DevicePlan& d, const HostPlan& hp);
 
 namespace {
 // The E-sized passes of the plan on the device (plan_device.cu) from the down CSR, uploaded
@@ -312,7 +311,8 @@ DevicePlan* ensure_device_plan(grgx_graph* g) {
     d->has_miss = hp.has_miss;
     for (uint32_t x : hp.xtx_new)
         if (x != COAL_NOT_SET) d->xtx_max = std::max(d->xtx_max, static_cast<double>(x));
-    build_up_split(*d, hp);
+    d->up_off = hp.up.off;
+    d->level_begin = hp.level_begin;
     g->dev = std::move(d);
     g->plan.reset();  // the device copy is authoritative; free the host copy
     return g->dev.get();
@@ -428,9 +428,7 @@ void matmul_direct(grgx_graph* g, int dtype, const void* input, uint64_t in_cols
         void* vals = sc.get(valBytes);
         // UP in split form when the height-0 rows outgrow L2: their edges first, in blocked
         // passes, then the other edges level by level (blocked.cu)
-        const bool split = !down && dp->up0b.n_rows > 0 &&
-                           static_cast<uint64_t>(dp->split_src) * static_cast<uint64_t>(L.stride) * L.ssize >
-                               blocked_threshold_bytes();
+        const bool split = !down && use_up_split(g, dp, L);
         long long pieces = down ? std::max(dp->down.n_pieces, std::max(dp->seed.n_pieces, dp->miss.n_pieces))
                                 : (split ? std::max(dp->up0b.n_pieces, dp->up_int.n_pieces) : dp->up.n_pieces);
         void* partials = sc.get(static_cast<size_t>(pieces) * L.stride * L.asize);
