@@ -8,7 +8,7 @@ The compute runs in libgrgx.so (hand-written sm_103a CUDA kernels behind a C ABI
 include/grgx.h); there is no CPU implementation in this package.
 """
 from .api import (COAL_COUNT_NOT_SET, DOWN, GRG, INVALID_NODE, UP, Server, TraversalDirection, autotune,
-                  autotune_clear, autotune_load, autotune_table, dot_product, from_csr, from_pygrgl, last_timing,
+                  autotune_clear, autotune_load, autotune_table, collect_timings, dot_product, from_csr, from_pygrgl, last_timing,
                   load_immutable_grg, matmul, matmul_batch, matmul_gram, matmul_standardized, measure_l2_bandwidth,
                   set_graph_replay, set_timing, window_tree_grg)
 
@@ -16,5 +16,5 @@ __all__ = [
     "COAL_COUNT_NOT_SET", "DOWN", "GRG", "INVALID_NODE", "UP", "TraversalDirection", "dot_product", "from_csr",
     "from_pygrgl", "last_timing", "load_immutable_grg", "matmul", "matmul_batch", "set_timing", "window_tree_grg",
     "Server", "matmul_standardized", "measure_l2_bandwidth", "set_graph_replay", "autotune", "autotune_table",
-    "autotune_load", "autotune_clear", "matmul_gram",
+    "autotune_load", "autotune_clear", "matmul_gram", "collect_timings",
 ]

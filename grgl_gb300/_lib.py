@@ -74,6 +74,7 @@ SIGNATURES = {
     "grgx_autotune_clear": (None, []),
     "grgx_set_timing": (None, [_int]),
     "grgx_last_timing": (_int, [ctypes.POINTER(Timing)]),
+    "grgx_collect_timings": (_int, [ctypes.POINTER(Timing), _u64, ctypes.POINTER(_u64)]),
 }
 
 _lib = None

@@ -391,9 +391,20 @@ def measure_l2_bandwidth(nbytes: int = 48 << 20, reps: int = 40) -> float:
     return v.value
 
 
-def set_timing(enabled: bool):
-    """Per-call CUDA-event timing on this thread (see last_timing)."""
-    _lib.lib().grgx_set_timing(int(bool(enabled)))
+def set_timing(enabled):
+    """Per-call CUDA-event timing on this thread: True (read back per call, see last_timing),
+    "deferred" (no per-call sync, see collect_timings) or False."""
+    _lib.lib().grgx_set_timing(2 if enabled == "deferred" else int(bool(enabled)))
+
+
+def collect_timings() -> list:
+    """The deferred timings of this thread's calls since the last collection, in call order."""
+    cap = 65536
+    buf = (_lib.Timing * cap)()
+    n = ctypes.c_uint64()
+    _lib.check(_lib.lib().grgx_collect_timings(buf, cap, ctypes.byref(n)))
+    return [{"total_ms": t.total_ms, "sweep_ms": t.sweep_ms, "launches": int(t.launches), "alg_bytes": int(t.alg_bytes)}
+            for t in buf[:n.value]]
 
 
 def last_timing() -> dict:

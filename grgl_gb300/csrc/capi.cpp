@@ -15,6 +15,7 @@ void matmul_impl(grgx_graph* g, int dtype, const void* input, uint64_t in_cols, 
                  void* miss, uint32_t flags, void* stream);
 void set_timing(int enabled);
 grgx_timing last_timing();
+std::vector<grgx_timing> collect_timings();
 double measure_l2_bandwidth(uint64_t bytes, int reps);
 void matmul_noalloc_impl(grgx_graph* g, int dtype, const void* input, uint64_t in_cols, uint64_t rows, int direction,
                          void* output, uint64_t output_size, void* stream);
@@ -393,6 +394,16 @@ extern "C" void grgx_debug_blocking(long long block, unsigned long long threshol
 double grgx_plan_benchmark(grgx_graph* g) {
     auto p = build_plan(g->host_edges());
     return static_cast<double>(p->up.adj.size());
+}
+
+grgx_status grgx_collect_timings(grgx_timing* out, uint64_t capacity, uint64_t* count) {
+    return guarded([&] {
+        GRGX_CHECK(count && (capacity == 0 || out), GRGX_ERR_API_MISUSE, "null argument");
+        const std::vector<grgx_timing> t = collect_timings();
+        GRGX_CHECK(t.size() <= capacity, GRGX_ERR_API_MISUSE, "timing buffer too small");
+        for (size_t i = 0; i < t.size(); i++) out[i] = t[i];
+        *count = t.size();
+    });
 }
 
 grgx_status grgx_last_timing(grgx_timing* out) {

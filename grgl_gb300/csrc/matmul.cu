@@ -136,8 +136,14 @@ struct Scratch {
     }
 };
 
-thread_local bool t_timing = false;
+thread_local int t_timing = 0;  // 0 off, 1 per call (synchronises), 2 deferred
 thread_local grgx_timing t_last{};
+// Deferred timing: each call's events, read back by collect_timings after the caller syncs.
+struct PendingTiming {
+    cudaEvent_t ev[4];
+    uint64_t launches, alg_bytes;
+};
+thread_local std::vector<PendingTiming> t_pending;
 
 }  // namespace
 
@@ -609,17 +615,22 @@ void matmul_direct(grgx_graph* g, int dtype, const void* input, uint64_t in_cols
     }  // scratch released (stream-ordered)
     if (t_timing) {
         GRGX_CUDA(cudaEventRecord(ev[3], s));
-        GRGX_CUDA(cudaEventSynchronize(ev[3]));
-        float tot = 0, sw = 0;
-        cudaEventElapsedTime(&tot, ev[0], ev[3]);
-        cudaEventElapsedTime(&sw, ev[1], ev[2]);
-        for (auto& e : ev) cudaEventDestroy(e);
         const DevCSR& c = down ? dp->down : dp->up;
-        t_last.total_ms = tot;
-        t_last.sweep_ms = sw;
-        t_last.launches = launches;
-        t_last.alg_bytes = static_cast<uint64_t>(c.n_edges) * (4 + static_cast<uint64_t>(K) * L.ssize) +
-                           static_cast<uint64_t>(c.n_rows) * (8 + static_cast<uint64_t>(K) * L.ssize);
+        const uint64_t algBytes = static_cast<uint64_t>(c.n_edges) * (4 + static_cast<uint64_t>(K) * L.ssize) +
+                                  static_cast<uint64_t>(c.n_rows) * (8 + static_cast<uint64_t>(K) * L.ssize);
+        if (t_timing == 2) {
+            t_pending.push_back(PendingTiming{{ev[0], ev[1], ev[2], ev[3]}, launches, algBytes});
+        } else {
+            GRGX_CUDA(cudaEventSynchronize(ev[3]));
+            float tot = 0, sw = 0;
+            cudaEventElapsedTime(&tot, ev[0], ev[3]);
+            cudaEventElapsedTime(&sw, ev[1], ev[2]);
+            for (auto& e : ev) cudaEventDestroy(e);
+            t_last.total_ms = tot;
+            t_last.sweep_ms = sw;
+            t_last.launches = launches;
+            t_last.alg_bytes = algBytes;
+        }
     } else {
         t_last.launches = launches;
     }
@@ -772,7 +783,24 @@ void clear_graph_replays(grgx_graph* g) {
     g->graphs.reset();
 }
 
-void set_timing(int enabled) { t_timing = enabled != 0; }
+void set_timing(int enabled) { t_timing = enabled == 2 ? 2 : (enabled != 0 ? 1 : 0); }
 grgx_timing last_timing() { return t_last; }
+
+// Reads back (waiting for them) and clears this thread's deferred timings, in call order.
+std::vector<grgx_timing> collect_timings() {
+    std::vector<grgx_timing> out;
+    for (PendingTiming& p : t_pending) {
+        grgx_timing t{};
+        cudaEventSynchronize(p.ev[3]);
+        cudaEventElapsedTime(&t.total_ms, p.ev[0], p.ev[3]);
+        cudaEventElapsedTime(&t.sweep_ms, p.ev[1], p.ev[2]);
+        for (auto& e : p.ev) cudaEventDestroy(e);
+        t.launches = p.launches;
+        t.alg_bytes = p.alg_bytes;
+        out.push_back(t);
+    }
+    t_pending.clear();
+    return out;
+}
 
 }  // namespace grgx

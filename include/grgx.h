@@ -295,9 +295,14 @@ typedef struct {
     uint64_t alg_bytes; /* algorithmic bytes of the sweep (edge ids + offsets + one row per edge + one row per node) */
 } grgx_timing;
 
-/* Enables per-call CUDA-event timing on this thread (adds a stream sync per call). */
+/* Per-call CUDA-event timing on this thread: 1 = read back at the end of each call (adds a
+ * stream sync per call; grgx_last_timing), 2 = deferred (no sync; grgx_collect_timings returns
+ * every call's timing, in call order, after waiting for them), 0 = off. */
 void grgx_set_timing(int enabled);
 grgx_status grgx_last_timing(grgx_timing* out);
+/* Deferred timings (grgx_set_timing(2)) of this thread's calls since the last collection; fails
+ * without clearing when there are more than `capacity`. */
+grgx_status grgx_collect_timings(grgx_timing* out, uint64_t capacity, uint64_t* count);
 
 #ifdef __cplusplus
 }

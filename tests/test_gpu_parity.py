@@ -322,3 +322,20 @@ def test_full_size_properties(gx):
         assert torch.equal(gx.matmul(g, 3 * a - 7 * b, d), 3 * gx.matmul(g, a, d) - 7 * gx.matmul(g, b, d))
     del g
     torch.cuda.empty_cache()
+
+
+def test_deferred_timing(gx, wt):
+    """Deferred timing records every call without synchronising; collection returns them in order."""
+    import torch
+
+    g, og = wt
+    V = torch.ones((4, og.num_samples), dtype=torch.float32, device="cuda")
+    gx.set_timing("deferred")
+    try:
+        for _ in range(3):
+            gx.matmul(g, V, UP)
+        ts = gx.collect_timings()
+    finally:
+        gx.set_timing(False)
+    assert len(ts) == 3 and all(t["total_ms"] >= t["sweep_ms"] > 0 and t["launches"] > 0 for t in ts)
+    assert gx.collect_timings() == []
