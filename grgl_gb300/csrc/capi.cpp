@@ -390,12 +390,6 @@ extern "C" void grgx_debug_blocking(long long block, unsigned long long threshol
     grgx::set_blocking(block, threshold_bytes);
 }
 
-// Host-only helper for profiling the plan build (not part of the public header).
-double grgx_plan_benchmark(grgx_graph* g) {
-    auto p = build_plan(g->host_edges());
-    return static_cast<double>(p->up.adj.size());
-}
-
 grgx_status grgx_collect_timings(grgx_timing* out, uint64_t capacity, uint64_t* count) {
     return guarded([&] {
         GRGX_CHECK(count && (capacity == 0 || out), GRGX_ERR_API_MISUSE, "null argument");
