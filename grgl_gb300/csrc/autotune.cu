@@ -143,7 +143,7 @@ std::string autotune_impl(grgx_graph* g, int dtype, uint64_t rows, int direction
     const Layout L = choose_layout(dtype, static_cast<long long>(rows), (flags & GRGX_FLAG_F32_PLAIN) != 0,
                                    (flags & GRGX_FLAG_F64_NATIVE) != 0);
     const bool down = (direction == GRGX_DIRECTION_DOWN);
-    // the CSRs a call of this shape sweeps: UP in split form (blocked.cu) when it would run so
+    // the CSRs a call of this shape sweeps: UP in split form (up_split.cu) when it would run so
     struct Pass {
         const DevCSR* c;
         int mode;

@@ -25,7 +25,7 @@ void matmul_standardized_impl(grgx_graph* g, int dtype, const void* input, uint6
                               int direction, void* output, uint64_t output_size, uint32_t flags, void* stream);
 void matmul_gram_impl(grgx_graph* g, int dtype, const void* input, uint64_t in_cols, uint64_t rows, int first,
                       void* output, uint64_t output_size, int standardized, uint32_t flags, void* stream);
-void set_blocking(long long block, unsigned long long thresholdBytes);
+void set_up_split(long long block, unsigned long long thresholdBytes);
 void* host_alloc(uint64_t bytes);
 void host_free(void* b);
 std::string autotune_impl(grgx_graph* g, int dtype, uint64_t rows, int direction, uint32_t flags);
@@ -384,10 +384,10 @@ extern "C" grgx_status grgx_graph_upload_host_plan(grgx_graph* g) {
     });
 }
 
-// Test hook (not part of the public header): the sample-block size used by plans built from now
-// on (0 keeps it) and the source-row bytes above which UP's first level runs blocked.
-extern "C" void grgx_debug_blocking(long long block, unsigned long long threshold_bytes) {
-    grgx::set_blocking(block, threshold_bytes);
+// Test hook (not part of the public header): the block of height-0 ids used by split copies
+// built from now on (0 keeps it) and the height-0 row bytes above which UP runs in split form.
+extern "C" void grgx_debug_up_split(long long block, unsigned long long threshold_bytes) {
+    grgx::set_up_split(block, threshold_bytes);
 }
 
 grgx_status grgx_collect_timings(grgx_timing* out, uint64_t capacity, uint64_t* count) {

@@ -102,15 +102,15 @@ int launch_level(const Layout& L, const DevCSR& c, size_t level, const void* src
                  int gateValue = 0, const LevelShape* shape = nullptr, int tileStride = 0, void* state = nullptr,
                  long long stateBase = 0, int stateMode = 1);
 
-// UP in split form (blocked.cu): writes vals[node] from its accumulator state (added onto the
+// UP in split form (up_split.cu): writes vals[node] from its accumulator state (added onto the
 // value when rmw) for the `count` nodes listed at `nodes`.
 void launch_state_finish(Kind kind, const void* state, void* vals, const int* nodes, long long count,
                          long long stateBase, long long stride, int rmw, cudaStream_t s, const int* gate,
                          int gateValue);
 // Height-0 row bytes (height-0 ids x stride x element size) above which UP runs in split form,
 // and the block of height-0 ids each split pass covers; both adjustable for tests.
-uint64_t blocked_threshold_bytes();
-long long blocked_block_size();
+uint64_t split_threshold_bytes();
+long long split_block_size();
 // Whether a call with layout L runs UP in split form; builds the split copy on first use.
 bool use_up_split(grgx_graph* g, DevicePlan* dp, const Layout& L);
 

@@ -433,7 +433,7 @@ void matmul_direct(grgx_graph* g, int dtype, const void* input, uint64_t in_cols
         const size_t valBytes = static_cast<size_t>(n) * L.stride * L.ssize;
         void* vals = sc.get(valBytes);
         // UP in split form when the height-0 rows outgrow L2: their edges first, in blocked
-        // passes, then the other edges level by level (blocked.cu)
+        // passes, then the other edges level by level (up_split.cu)
         const bool split = !down && use_up_split(g, dp, L);
         long long pieces = down ? std::max(dp->down.n_pieces, std::max(dp->seed.n_pieces, dp->miss.n_pieces))
                                 : (split ? std::max(dp->up0b.n_pieces, dp->up_int.n_pieces) : dp->up.n_pieces);

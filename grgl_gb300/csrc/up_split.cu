@@ -151,10 +151,10 @@ DevCSR upload_pull(DevicePlan& d, PullCSR& P, uint32_t* adj, long long E) {
 
 }  // namespace
 
-uint64_t blocked_threshold_bytes() { return g_threshold.load(); }
-long long blocked_block_size() { return g_block.load(); }
+uint64_t split_threshold_bytes() { return g_threshold.load(); }
+long long split_block_size() { return g_block.load(); }
 
-void set_blocking(long long block, unsigned long long thresholdBytes) {
+void set_up_split(long long block, unsigned long long thresholdBytes) {
     if (block > 0) g_block.store(block);
     g_threshold.store(thresholdBytes);
 }
@@ -179,7 +179,7 @@ namespace {
 // Builds d.up0b / d.up_int / d.fin from the resident UP CSR (rows = nodes level_begin[1] .. n-1
 // in order, children ascending).
 void build_up_split(DevicePlan& d) {
-    const long long block = blocked_block_size();
+    const long long block = split_block_size();
     const long long src0 = static_cast<long long>(d.level_begin[1]);
     const long long n = static_cast<long long>(d.level_begin[d.num_levels]);
     const long long R = n - src0;
@@ -300,7 +300,7 @@ void build_up_split(DevicePlan& d) {
 bool use_up_split(grgx_graph* g, DevicePlan* dp, const Layout& L) {
     if (dp->num_levels < 2 || dp->level_begin.size() < 2) return false;
     const long long src0 = static_cast<long long>(dp->level_begin[1]);
-    if (static_cast<uint64_t>(src0) * static_cast<uint64_t>(L.stride) * L.ssize <= blocked_threshold_bytes())
+    if (static_cast<uint64_t>(src0) * static_cast<uint64_t>(L.stride) * L.ssize <= split_threshold_bytes())
         return false;
     {
         std::lock_guard<std::mutex> lk(g->mu);

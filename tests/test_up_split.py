@@ -14,10 +14,10 @@ DOWN, UP = 1, 2
 DEFAULT_BLOCK, DEFAULT_THRESHOLD = 32768, 96 << 20
 
 
-def _blocking(block, threshold):
+def _split_knobs(block, threshold):
     from grgl_gb300 import _lib
 
-    fn = _lib.lib().grgx_debug_blocking
+    fn = _lib.lib().grgx_debug_up_split
     fn.restype = None
     fn.argtypes = [ctypes.c_longlong, ctypes.c_ulonglong]
     fn(block, threshold)
@@ -27,7 +27,7 @@ def _blocking(block, threshold):
 def env(cuda_ok):
     import grgl_gb300 as gx
 
-    _blocking(256, 0)  # plans built now are cut every 256 height-0 ids; every UP call runs split
+    _split_knobs(256, 0)  # plans built now are cut every 256 height-0 ids; every UP call runs split
     try:
         g = gx.window_tree_grg(3000, 20000, seed=91).upload()
         a = g.export_arrays()
@@ -35,7 +35,7 @@ def env(cuda_ok):
                                 mut_node=a["mut_node"])
         yield gx, g, og
     finally:
-        _blocking(DEFAULT_BLOCK, DEFAULT_THRESHOLD)
+        _split_knobs(DEFAULT_BLOCK, DEFAULT_THRESHOLD)
 
 
 def _check(got, ref, scale, dt):
@@ -94,9 +94,9 @@ def test_split_equals_unsplit_for_integers(env):
     gx, g, og = env
     V = np.random.default_rng(5).integers(-9, 9, size=(33, g.num_samples)).astype(np.int32)
     blocked = gx.matmul(g, V, UP)
-    _blocking(0, 1 << 62)  # same plan, every call on the unsplit UP CSR
+    _split_knobs(0, 1 << 62)  # same plan, every call on the unsplit UP CSR
     try:
         plain = gx.matmul(g, V, UP)
     finally:
-        _blocking(0, 0)
+        _split_knobs(0, 0)
     assert np.array_equal(blocked, plain)
