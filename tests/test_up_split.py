@@ -11,7 +11,7 @@ import oracle
 
 pytestmark = pytest.mark.gpu
 DOWN, UP = 1, 2
-DEFAULT_BLOCK, DEFAULT_THRESHOLD = 32768, 96 << 20
+DEFAULT_BLOCK, DEFAULT_THRESHOLD = 32768, 64 << 20
 
 
 def _split_knobs(block, threshold):
@@ -27,7 +27,7 @@ def _split_knobs(block, threshold):
 def env(cuda_ok):
     import grgl_gb300 as gx
 
-    _split_knobs(256, 0)  # plans built now are cut every 256 height-0 ids; every UP call runs split
+    _split_knobs(256, 0)  # split copies built now cut every 256 height-0 ids; every UP call runs split
     try:
         g = gx.window_tree_grg(3000, 20000, seed=91).upload()
         a = g.export_arrays()
