@@ -261,7 +261,7 @@ def served(gx, graphs, rate, seconds, max_requests, rng):
         t += rng.exponential(1.0 / rate)
         if t > seconds:
             break
-        gi = 0 if rng.random() < 0.7 else 1
+        gi = 0 if (len(graphs) == 1 or rng.random() < 0.7) else 1
         K = int(np.exp(rng.uniform(0.0, np.log(256.0))))
         d = UP if rng.random() < 0.5 else DOWN
         dt = "int32" if rng.random() < 0.5 else "float32"
@@ -414,12 +414,14 @@ def large_graph(gx, torch, args, peak):
                "edgeK_per_s": b_units / t_b, "alg_GBps": b_bytes / t_b / 1e9, "hbm_frac": b_bytes / t_b / 1e9 / peak,
                "mix": "K~U{1..128}, UP/DOWN 50/50, float32 compensated, device inputs"}
     del reqs
+    # and served: Poisson arrivals at 1000 req/s, the serving mix, on this graph alone
+    serve = served(gx, [g], 1000.0, 1.0, 48, rng)
     del g
     torch.cuda.empty_cache()
     return {"graph": dict(stats, note=f"variant prefix M'={args.large_mutations} of the 10,000,000-variant "
                                       "generator run, sized to the 2-4e9-edge budget"),
             "edgeK_per_s": units / secs, "alg_GBps": abytes / secs / 1e9, "hbm_frac": abytes / secs / 1e9 / peak,
-            "matmuls": rows, "batched": batched,
+            "matmuls": rows, "batched": batched, "served": serve,
             "setup_s": {"generate": t_gen, "plan_upload": t_up, "autotune": t_tune}}
 
 
