@@ -10,7 +10,9 @@
 // resident graph (CUDA events around the level's launch, best of two after a warm launch) --
 // the deep variant at the default lanes, then halvings of the lanes per row while each keeps
 // winning -- and records the winner when it beats the default by more than 2%.  Levels with
-// under 0.5% of the traversal's edges keep the default.  Calls on any graph then look up every
+// under 0.5% of the traversal's edges keep the default.  For UP on graphs where the split form
+// (up_split.cu) is possible it tunes both forms and records, for this graph and (storage kind,
+// stride), the one whose tuned sweep is faster.  Calls on any graph then look up every
 // level's key; levels without an entry run the default shape.  Shapes change only the order in
 // which a row's float terms are added (integer results are bit-exact with any shape).
 #include <cuda_runtime.h>
@@ -143,27 +145,32 @@ std::string autotune_impl(grgx_graph* g, int dtype, uint64_t rows, int direction
     const Layout L = choose_layout(dtype, static_cast<long long>(rows), (flags & GRGX_FLAG_F32_PLAIN) != 0,
                                    (flags & GRGX_FLAG_F64_NATIVE) != 0);
     const bool down = (direction == GRGX_DIRECTION_DOWN);
-    // the CSRs a call of this shape sweeps: UP in split form (up_split.cu) when it would run so
+    // the CSRs a call of this shape sweeps; for UP both forms when the split form is possible,
+    // so the faster one is recorded for this graph
     struct Pass {
         const DevCSR* c;
         int mode;
         const char* name;
     };
-    std::vector<Pass> passes;
-    const bool split = !down && use_up_split(g, dp, L);
-    if (down) passes.push_back({&dp->down, 0, "level"});
-    else if (split) {
-        passes.push_back({&dp->up0b, 1, "height-0 block"});
-        passes.push_back({&dp->up_int, 2, "level"});
+    std::vector<std::vector<Pass>> forms;
+    const bool trySplit = !down && up_split_possible(dp);
+    if (down) {
+        forms.push_back({{&dp->down, 0, "level"}});
     } else {
-        passes.push_back({&dp->up, 0, "level"});
+        forms.push_back({{&dp->up, 0, "level"}});
+        if (trySplit) {
+            ensure_up_split(g, dp);
+            if (dp->up0b.n_rows > 0)
+                forms.push_back({{&dp->up0b, 1, "split: height-0 block"}, {&dp->up_int, 2, "split: level"}});
+        }
     }
-    long long maxPieces = 0, maxHeavy = 0, totalEdges = 0;
-    for (const Pass& ps : passes) {
-        maxPieces = std::max(maxPieces, ps.c->n_pieces);
-        maxHeavy = std::max(maxHeavy, ps.c->n_heavy);
-        totalEdges += ps.c->n_edges;
-    }
+    long long maxPieces = 0, maxHeavy = 0;
+    for (const auto& f : forms)
+        for (const Pass& ps : f) {
+            maxPieces = std::max(maxPieces, ps.c->n_pieces);
+            maxHeavy = std::max(maxHeavy, ps.c->n_heavy);
+        }
+    const bool needState = forms.size() > 1;
     const int maxT = max_tiles(L);
     const size_t n = g->host->num_nodes;
     cudaStream_t s = nullptr;
@@ -186,7 +193,7 @@ std::string autotune_impl(grgx_graph* g, int dtype, uint64_t rows, int direction
         GRGX_CUDA(cudaMalloc(&vals, std::max<size_t>(valBytes, 16)));
         GRGX_CUDA(cudaMemsetAsync(vals, 0, valBytes, s));
         GRGX_CUDA(cudaMalloc(&partials, std::max<size_t>(static_cast<size_t>(maxPieces) * L.stride * L.asize, 16)));
-        if (split) {
+        if (needState) {
             const size_t stateBytes = (n - static_cast<size_t>(dp->split_src)) * L.stride * std::max(L.asize, 8);
             GRGX_CUDA(cudaMalloc(&state, std::max<size_t>(stateBytes, 16)));
             GRGX_CUDA(cudaMemsetAsync(state, 0, stateBytes, s));
@@ -217,55 +224,71 @@ std::string autotune_impl(grgx_graph* g, int dtype, uint64_t rows, int direction
             return best;
         };
         const std::vector<int> gs = candidate_g(L);
-        double totDefault = 0, totBest = 0;
-        for (const Pass& ps : passes) {
-        cur = ps.c;
-        curMode = ps.mode;
-        const DevCSR& c = *ps.c;
-        for (size_t lvl = 0; lvl < c.lb.size(); lvl++) {
-            if (c.le[lvl] <= c.lb[lvl]) continue;
-            // levels under 0.5% of the traversal's edges keep the default untimed
-            if (c.level_edges[lvl] * 200 < totalEdges) continue;
-            const LevelShape def = default_shape(L);
-            const float tDef = time_shape(lvl, def);
-            LevelShape best = def;
-            float tBest = tDef;
-            // greedy: the deep variant at the default lanes, then fewer lanes per row with the
-            // better variant while each halving keeps winning by 2%
-            if (has_deep(L)) {
-                const LevelShape deep{def.g, def.ntiles, 1};
-                const float t = time_shape(lvl, deep);
-                if (t < 0.98f * tBest) {
-                    tBest = t;
-                    best = deep;
+        std::vector<double> formBest;
+        for (const auto& form : forms) {
+            long long totalEdges = 0;
+            for (const Pass& ps : form) totalEdges += ps.c->n_edges;
+            double totDefault = 0, totBest = 0;
+            for (const Pass& ps : form) {
+                cur = ps.c;
+                curMode = ps.mode;
+                const DevCSR& c = *ps.c;
+                for (size_t lvl = 0; lvl < c.lb.size(); lvl++) {
+                    if (c.le[lvl] <= c.lb[lvl]) continue;
+                    const LevelShape def = default_shape(L);
+                    const float tDef = time_shape(lvl, def);
+                    totDefault += tDef;
+                    // levels under 0.5% of the traversal's edges keep the default
+                    if (c.level_edges[lvl] * 200 < totalEdges) {
+                        totBest += tDef;
+                        continue;
+                    }
+                    LevelShape best = def;
+                    float tBest = tDef;
+                    // greedy: the deep variant at the default lanes, then fewer lanes per row with
+                    // the better variant while each halving keeps winning by 2%
+                    if (has_deep(L)) {
+                        const LevelShape deep{def.g, def.ntiles, 1};
+                        const float t = time_shape(lvl, deep);
+                        if (t < 0.98f * tBest) {
+                            tBest = t;
+                            best = deep;
+                        }
+                    }
+                    for (size_t i = 1; i < gs.size(); i++) {
+                        const LevelShape sh{gs[i], tiles_for(L, gs[i]), best.variant};
+                        const float t = time_shape(lvl, sh);
+                        if (!(t < 0.98f * tBest)) break;
+                        tBest = t;
+                        best = sh;
+                    }
+                    totBest += tBest;
+                    {
+                        std::lock_guard<std::mutex> lk(g_table_mu);
+                        g_table[key_for(L, c.level_rows[lvl], c.level_edges[lvl])] = best;
+                        g_table_nonempty.store(true, std::memory_order_release);
+                    }
+                    char line[256];
+                    std::snprintf(line, sizeof(line),
+                                  "%s %zu rows %lld edges %lld: g %d tiles %d variant %d, %.4f ms (default g %d "
+                                  "variant 0: %.4f ms)\n",
+                                  ps.name, lvl, c.level_rows[lvl], c.level_edges[lvl], best.g, best.ntiles,
+                                  best.variant, tBest, def.g, tDef);
+                    rep << line;
                 }
             }
-            for (size_t i = 1; i < gs.size(); i++) {
-                const LevelShape sh{gs[i], tiles_for(L, gs[i]), best.variant};
-                const float t = time_shape(lvl, sh);
-                if (!(t < 0.98f * tBest)) break;
-                tBest = t;
-                best = sh;
-            }
-            totDefault += tDef;
-            totBest += tBest;
-            {
-                std::lock_guard<std::mutex> lk(g_table_mu);
-                g_table[key_for(L, c.level_rows[lvl], c.level_edges[lvl])] = best;
-                g_table_nonempty.store(true, std::memory_order_release);
-            }
-            char line[256];
-            std::snprintf(line, sizeof(line),
-                          "%s %zu rows %lld edges %lld: g %d tiles %d variant %d, %.4f ms (default g %d variant "
-                          "0: %.4f ms)\n",
-                          ps.name, lvl, c.level_rows[lvl], c.level_edges[lvl], best.g, best.ntiles, best.variant,
-                          tBest, def.g, tDef);
-            rep << line;
+            char tail[160];
+            std::snprintf(tail, sizeof(tail), "%s %.4f ms tuned, %.4f ms default\n",
+                          forms.size() > 1 ? (form[0].mode ? "split sweep" : "unsplit sweep") : "sweep", totBest,
+                          totDefault);
+            rep << tail;
+            formBest.push_back(totBest);
         }
+        if (forms.size() > 1) {
+            const bool split = formBest[1] < 0.98 * formBest[0];
+            set_up_split_choice(g, dp, L, split);
+            rep << (split ? "UP runs in split form for this shape\n" : "UP runs unsplit for this shape\n");
         }
-        char tail[160];
-        std::snprintf(tail, sizeof(tail), "sweep %.4f ms tuned, %.4f ms default\n", totBest, totDefault);
-        rep << tail;
     } catch (...) {
         release();
         throw;

@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <map>
 #include <string>
 #include <vector>
 
@@ -46,6 +47,7 @@ struct DevicePlan {
     std::vector<long long> fin_begin;
     long long split_block = 0, split_src = 0;  // split_src = height-0 ids = first UP row's node id
     bool split_built = false;
+    std::map<std::pair<int, long long>, bool> split_choice;  // (storage kind, stride) -> measured choice
     std::vector<int64_t> up_off;         // UP row offsets (host copy)
     std::vector<uint64_t> level_begin;   // node-id range of each height
     uint32_t* mut_new = nullptr;
@@ -111,8 +113,13 @@ void launch_state_finish(Kind kind, const void* state, void* vals, const int* no
 // and the block of height-0 ids each split pass covers; both adjustable for tests.
 uint64_t split_threshold_bytes();
 long long split_block_size();
-// Whether a call with layout L runs UP in split form; builds the split copy on first use.
+// Whether a call with layout L runs UP in split form: the choice grgx_autotune measured for
+// (storage kind, stride) on this graph, else whether the height-0 rows exceed the threshold.
+// Builds the split copy on first use.
 bool use_up_split(grgx_graph* g, DevicePlan* dp, const Layout& L);
+bool up_split_possible(const DevicePlan* dp);
+void ensure_up_split(grgx_graph* g, DevicePlan* dp);
+void set_up_split_choice(grgx_graph* g, DevicePlan* dp, const Layout& L, bool split);
 
 // Builds (once) and returns the graph's plan on the current device.
 DevicePlan* ensure_device_plan(grgx_graph* g);

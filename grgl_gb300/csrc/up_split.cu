@@ -20,6 +20,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <map>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -297,18 +298,41 @@ void build_up_split(DevicePlan& d) {
 }
 }  // namespace
 
-bool use_up_split(grgx_graph* g, DevicePlan* dp, const Layout& L) {
+bool up_split_possible(const DevicePlan* dp) {
     if (dp->num_levels < 2 || dp->level_begin.size() < 2) return false;
     const long long src0 = static_cast<long long>(dp->level_begin[1]);
-    if (static_cast<uint64_t>(src0) * static_cast<uint64_t>(L.stride) * L.ssize <= split_threshold_bytes())
-        return false;
+    const long long block = split_block_size();
+    return (src0 + block - 1) / block >= 2;
+}
+
+void ensure_up_split(grgx_graph* g, DevicePlan* dp) {
+    std::lock_guard<std::mutex> lk(g->mu);
+    if (!dp->split_built) {
+        build_up_split(*dp);
+        dp->split_built = true;
+    }
+}
+
+void set_up_split_choice(grgx_graph* g, DevicePlan* dp, const Layout& L, bool split) {
+    std::lock_guard<std::mutex> lk(g->mu);
+    dp->split_choice[{static_cast<int>(L.kind), L.stride}] = split;
+}
+
+bool use_up_split(grgx_graph* g, DevicePlan* dp, const Layout& L) {
+    if (!up_split_possible(dp)) return false;
+    bool want;
     {
         std::lock_guard<std::mutex> lk(g->mu);
-        if (!dp->split_built) {
-            build_up_split(*dp);
-            dp->split_built = true;
+        auto it = dp->split_choice.find({static_cast<int>(L.kind), L.stride});
+        if (it != dp->split_choice.end()) {
+            want = it->second;  // measured by grgx_autotune on this graph
+        } else {
+            const long long src0 = static_cast<long long>(dp->level_begin[1]);
+            want = static_cast<uint64_t>(src0) * static_cast<uint64_t>(L.stride) * L.ssize > split_threshold_bytes();
         }
     }
+    if (!want) return false;
+    ensure_up_split(g, dp);
     return dp->up0b.n_rows > 0;
 }
 

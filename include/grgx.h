@@ -274,7 +274,9 @@ void grgx_host_free(void* p);
  * (`flags`: GRGX_FLAG_F32_PLAIN / GRGX_FLAG_F64_NATIVE select the accumulator as in
  * grgx_matmul): the deep variant, then fewer lanes per row while that keeps winning; levels
  * with under 0.5% of the edges keep the default.  It records each level's winner when it beats
- * the default by more than 2%, and
+ * the default by more than 2%.  For UP on graphs with enough samples it tunes both the plain
+ * level sweep and the split form (edges to samples first, in sample blocks) and records for
+ * `g` and this row width which form is faster.  It
  * writes a per-level report to `report` (NUL-terminated, truncated to `report_len`;
  * `report_needed`, if not NULL, gets the full size).  It drops `g`'s captured CUDA graphs; make
  * no other call on `g` while it runs.  Float results may round differently under another shape
