@@ -100,3 +100,41 @@ def test_split_equals_unsplit_for_integers(env):
     finally:
         _split_knobs(0, 0)
     assert np.array_equal(blocked, plain)
+
+
+def test_split_built_lazily_under_concurrent_calls(cuda_ok):
+    """Threads that all make the graph's first UP call at once share one split copy and get the
+    single-threaded results."""
+    import threading
+
+    import torch
+
+    import grgl_gb300 as gx
+
+    _split_knobs(256, 0)
+    try:
+        g = gx.window_tree_grg(2500, 9000, seed=93).upload()
+        rng = np.random.default_rng(6)
+        Vs = [rng.integers(-20, 20, size=(5, g.num_samples)).astype(np.int32) for _ in range(6)]
+        outs = [None] * 6
+        errs = []
+
+        def work(i):
+            try:
+                outs[i] = gx.matmul(g, torch.from_numpy(Vs[i]).cuda(), UP).cpu().numpy()
+            except Exception as e:  # reported below
+                errs.append(e)
+
+        th = [threading.Thread(target=work, args=(i,)) for i in range(6)]
+        for t in th:
+            t.start()
+        for t in th:
+            t.join()
+        assert not errs, errs
+        a = g.export_arrays()
+        og = oracle.OracleGraph(num_samples=2500, ploidy=2, down_off=a["down_off"], down_adj=a["down_adj"],
+                                mut_node=a["mut_node"])
+        for V, out in zip(Vs, outs):
+            assert np.array_equal(out, oracle.matmul(og, V, UP))
+    finally:
+        _split_knobs(DEFAULT_BLOCK, DEFAULT_THRESHOLD)
