@@ -53,12 +53,12 @@ def cases_for(N: int, M: int, n: int, ploidy: int, has_miss: bool = False, profi
             kw["miss"] = _values(rng, dtype, (K, M))
         out.append((name, (V, direction, kw)))
 
-    # the config-1 workload (DOWN int32 ones, DOWN/UP f64 N(0,1), K=1)
+    # allele counts and single float64 vectors: DOWN int32 ones, DOWN/UP float64 N(0,1), K=1
     add("down_i32_ones_k1", np.int32, 1, DOWN, ones=True)
     add("up_i32_ones_k1", np.int32, 1, UP, ones=True)
     add("down_f64_k1", np.float64, 1, DOWN)
     add("up_f64_k1", np.float64, 1, UP)
-    if profile == "wt_n1000_m10000":
+    if profile == "k1":
         return out
     if has_miss:
         add("down_f64_miss_k2", np.float64, 2, DOWN, miss="input")

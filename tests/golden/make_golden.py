@@ -78,6 +78,11 @@ def write_vcf(X: np.ndarray, path: Path):
 
 
 def main():
+    if sys.argv[1:] == ["--window-tree-only"]:
+        # re-record the window-tree fixture's outputs from its existing .grg
+        record(HERE / "wt_n1000_m10000.grg", HERE / "wt_n1000_m10000.npz",
+               {"generator": "window_tree N=1000 M=10000 seed=42 window=100"}, "full")
+        return
     # 1. the reference's 200-sample test input
     t200 = HERE / "t200.grg"
     construct(REF / "test/endtoend/input/test-200-samples.vcf.gz", t200)
@@ -92,7 +97,7 @@ def main():
     construct(REF / "test/endtoend/input/test-200-samples.miss.igd", t200m)
     record(t200m, HERE / "t200miss.npz", {"miss": True}, "miss")
 
-    # 3. config-1 workload: seeded window-tree genotypes -> VCF -> reference constructor
+    # 3. seeded window-tree genotypes (N=1,000, M=10,000) -> VCF -> reference constructor
     import oracle
     import grgl_gb300
 
@@ -106,7 +111,7 @@ def main():
     write_vcf(X, vcf)
     construct(vcf, HERE / "wt_n1000_m10000.grg")
     record(HERE / "wt_n1000_m10000.grg", HERE / "wt_n1000_m10000.npz", {"generator": "window_tree N=1000 M=10000 seed=42 window=100",
-                                                  "nnz": int(X.sum())}, "wt_n1000_m10000")
+                                                  "nnz": int(X.sum())}, "full")
 
 
 if __name__ == "__main__":
