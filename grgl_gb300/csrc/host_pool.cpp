@@ -4,10 +4,11 @@
 // device-to-host copy of a large result then pays at a fraction of the link's bandwidth.  Blocks
 // from cudaHostAlloc are faulted in and pinned once and the copy engine writes them at full
 // speed, so the library hands out pinned blocks for host results and keeps freed ones (by
-// power-of-two size class, up to kCacheBytes in all) for the next call.
+// power-of-two size class, up to cache_bytes() in all) for the next call.
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <cstdlib>
 #include <map>
 #include <mutex>
 #include <unordered_map>
@@ -20,7 +21,15 @@ namespace grgx {
 namespace {
 
 constexpr uint64_t kMinClass = 1ull << 20;
-constexpr uint64_t kCacheBytes = 16ull << 30;
+
+// Bytes of freed blocks kept for reuse: 16 GiB, or GRGX_HOST_POOL_BYTES when set.
+uint64_t cache_bytes() {
+    static const uint64_t v = [] {
+        const char* e = std::getenv("GRGX_HOST_POOL_BYTES");
+        return e ? std::strtoull(e, nullptr, 10) : (16ull << 30);
+    }();
+    return v;
+}
 
 struct HostPool {
     std::mutex mu;
@@ -78,7 +87,7 @@ void host_free(void* b) {
         if (it == p.live.end()) return;  // not ours
         cls = it->second;
         p.live.erase(it);
-        if (p.cached + cls <= kCacheBytes) {
+        if (p.cached + cls <= cache_bytes()) {
             p.free[cls].push_back(b);
             p.cached += cls;
             return;

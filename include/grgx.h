@@ -257,8 +257,9 @@ grgx_status grgx_measure_l2_bandwidth(uint64_t bytes, int reps, double* gbps);
 /* No counterpart in the reference.  Page-locked host memory for results the caller will have
  * copied back (grgx_matmul / batch / server outputs in host memory): device-to-host copies
  * into it run at the link's full speed, while a freshly allocated pageable buffer pays a page
- * fault per page during the copy.  Freed blocks are cached by power-of-two size (16 GiB in
- * all) for later calls.  grgx_host_free ignores pointers it did not hand out. */
+ * fault per page during the copy.  Freed blocks are cached by power-of-two size for later calls
+ * (16 GiB in all, or the GRGX_HOST_POOL_BYTES environment variable).  grgx_host_free ignores
+ * pointers it did not hand out. */
 grgx_status grgx_host_alloc(uint64_t bytes, void** out);
 void grgx_host_free(void* p);
 
