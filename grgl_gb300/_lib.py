@@ -15,6 +15,7 @@ OK, ERR_API_MISUSE, ERR_CUDA, ERR_OOM, ERR_BAD_FILE, ERR_UNSUPPORTED, ERR_NO_DEV
 FLAG_DEVICE_POINTERS, FLAG_F32_PLAIN, FLAG_SYNC, FLAG_OVERWRITE, FLAG_F64_NATIVE = 0x1, 0x2, 0x4, 0x8, 0x10
 FLAG_NO_GRAPH = 0x20
 REQUEST_STANDARDIZED = 0x1
+REQUEST_BY_INDIVIDUAL = 0x2
 NOALLOC_SCRATCH_BYTES = 64 << 20  # GRGX_NOALLOC_SCRATCH_BYTES
 
 # Every symbol include/grgx.h declares, with its ctypes signature.

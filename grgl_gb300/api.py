@@ -478,12 +478,14 @@ def matmul_gram(grg: GRG, input, first_direction, *, standardized: bool = False,
 # ---- batching and serving ----------------------------------------------------------------------
 
 
-def _request_for(grg, x, direction, standardized=False):
+def _request_for(grg, x, direction, standardized=False, by_individual=False):
     """Validate one request and allocate its output (host or device like the input)."""
     direction = TraversalDirection(int(direction))
-    opts = _lib.REQUEST_STANDARDIZED if standardized else 0
-    cols = grg.num_samples if direction == UP else grg.num_mutations
-    out_cols = grg.num_mutations if direction == UP else grg.num_samples
+    opts = (_lib.REQUEST_STANDARDIZED if standardized else 0) | (_lib.REQUEST_BY_INDIVIDUAL if by_individual else 0)
+    _check(not (standardized and by_individual), "standardized products are per haplotype (no by_individual)")
+    nsamp = grg.num_individuals if by_individual else grg.num_samples
+    cols = nsamp if direction == UP else grg.num_mutations
+    out_cols = grg.num_mutations if direction == UP else nsamp
     if _is_torch_cuda(x):
         import torch
 
@@ -549,13 +551,15 @@ def autotune_clear() -> None:
 def matmul_batch(grg: GRG, requests, max_cols: int = 0, *, f32_compensated: bool = True, f64_native: bool = False):
     """Several products on one graph, coalesced into shared traversals.
 
-    ``requests`` is a list of ``(input, direction)`` or ``(input, direction, standardized)``;
-    inputs are all numpy arrays or all CUDA tensors.  A standardized request computes what
-    ``matmul_standardized`` does.  Returns the outputs in order.  Requests of the same direction
+    ``requests`` is a list of ``(input, direction)``, ``(input, direction, standardized)`` or
+    ``(input, direction, standardized, by_individual)``; inputs are all numpy arrays or all CUDA
+    tensors.  A standardized request computes what ``matmul_standardized`` does; by_individual
+    has ``matmul``'s meaning.  Returns the outputs in order.  Requests of the same direction
     and dtype are stacked into traversals of at most ``max_cols`` rows (0 = 512 for 4-byte and
     smaller dtypes, 256 for 8-byte ones).
     """
-    prepared = [_request_for(grg, r[0], r[1], bool(r[2]) if len(r) > 2 else False) for r in requests]
+    prepared = [_request_for(grg, r[0], r[1], bool(r[2]) if len(r) > 2 else False,
+                             bool(r[3]) if len(r) > 3 else False) for r in requests]
     if not prepared:
         return []
     dev = _is_torch_cuda(prepared[0][0])
@@ -593,8 +597,8 @@ class Server:
         self._graphs.append(grg)
         return int(gid.value)
 
-    def submit(self, graph_id: int, input, direction, standardized: bool = False) -> int:
-        x, out, req = _request_for(self._graphs[graph_id], input, direction, standardized)
+    def submit(self, graph_id: int, input, direction, standardized: bool = False, by_individual: bool = False) -> int:
+        x, out, req = _request_for(self._graphs[graph_id], input, direction, standardized, by_individual)
         _check(not _is_torch_cuda(x), "the server takes host (numpy) arrays")
         t = ctypes.c_uint64()
         _lib.check(_lib.lib().grgx_server_submit(self._h, graph_id, ctypes.byref(req), ctypes.byref(t)))

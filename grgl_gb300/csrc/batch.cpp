@@ -10,6 +10,7 @@
 #include <algorithm>
 #include <map>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "grgx_internal.h"
@@ -62,25 +63,33 @@ void matmul_batch_impl(grgx_graph* g, const grgx_request* reqs, uint64_t n, uint
     const HostGraph& hg = *g->host;
     const bool dev = (flags & GRGX_FLAG_DEVICE_POINTERS) != 0;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    // group by (direction, dtype), keeping submission order inside a group
-    std::map<std::pair<int, int>, std::vector<uint64_t>> groups;
+    // group by (direction, dtype, by_individual), keeping submission order inside a group
+    std::map<std::tuple<int, int, int>, std::vector<uint64_t>> groups;
     for (uint64_t i = 0; i < n; i++) {
         const grgx_request& r = reqs[i];
         GRGX_CHECK(r.input && r.output && r.rows > 0, GRGX_ERR_API_MISUSE, "matmul() requires non-zero dimensions.");
         GRGX_CHECK(r.direction == GRGX_DIRECTION_DOWN || r.direction == GRGX_DIRECTION_UP, GRGX_ERR_API_MISUSE,
                    "Invalid traversal direction");
         GRGX_CHECK(r.dtype >= GRGX_F64 && r.dtype <= GRGX_BOOL, GRGX_ERR_API_MISUSE, "Unsupported dtype");
-        GRGX_CHECK((r.options & ~GRGX_REQUEST_STANDARDIZED) == 0, GRGX_ERR_API_MISUSE, "Unknown request options");
+        GRGX_CHECK((r.options & ~(GRGX_REQUEST_STANDARDIZED | GRGX_REQUEST_BY_INDIVIDUAL)) == 0, GRGX_ERR_API_MISUSE,
+                   "Unknown request options");
         GRGX_CHECK(!(r.options & GRGX_REQUEST_STANDARDIZED) || r.dtype == GRGX_F32 || r.dtype == GRGX_F64,
                    GRGX_ERR_UNSUPPORTED, "standardized products take float32 or float64 input");
-        groups[{static_cast<int>(r.direction), static_cast<int>(r.dtype)}].push_back(i);
+        GRGX_CHECK(!((r.options & GRGX_REQUEST_STANDARDIZED) && (r.options & GRGX_REQUEST_BY_INDIVIDUAL)),
+                   GRGX_ERR_UNSUPPORTED, "standardized products are per haplotype (no by_individual)");
+        GRGX_CHECK(!(r.options & GRGX_REQUEST_BY_INDIVIDUAL) || hg.num_samples % hg.ploidy == 0, GRGX_ERR_API_MISUSE,
+                   "by_individual needs the number of samples to be a multiple of the ploidy");
+        groups[{static_cast<int>(r.direction), static_cast<int>(r.dtype),
+                (r.options & GRGX_REQUEST_BY_INDIVIDUAL) ? 1 : 0}]
+            .push_back(i);
     }
     const uint32_t passFlags = (flags & (GRGX_FLAG_F32_PLAIN | GRGX_FLAG_F64_NATIVE)) | GRGX_FLAG_DEVICE_POINTERS |
                                GRGX_FLAG_OVERWRITE;
     for (auto& kv : groups) {
-        const int direction = kv.first.first, dtype = kv.first.second;
-        const uint64_t cols = (direction == GRGX_DIRECTION_UP) ? hg.num_samples : hg.num_mutations;
-        const uint64_t outCols = (direction == GRGX_DIRECTION_UP) ? hg.num_mutations : hg.num_samples;
+        const int direction = std::get<0>(kv.first), dtype = std::get<1>(kv.first), byIndiv = std::get<2>(kv.first);
+        const uint64_t sampleCols = byIndiv ? hg.num_samples / hg.ploidy : hg.num_samples;
+        const uint64_t cols = (direction == GRGX_DIRECTION_UP) ? sampleCols : hg.num_mutations;
+        const uint64_t outCols = (direction == GRGX_DIRECTION_UP) ? hg.num_mutations : sampleCols;
         const size_t es = elem_bytes(dtype);
         const uint64_t width = maxCols ? maxCols : default_batch_cols(dtype);
         const std::vector<uint64_t>& idx = kv.second;
@@ -97,7 +106,7 @@ void matmul_batch_impl(grgx_graph* g, const grgx_request* reqs, uint64_t n, uint
                     matmul_standardized_impl(g, dtype, r.input, cols, r.rows, direction, r.output, r.rows * outCols,
                                              flags & ~GRGX_FLAG_SYNC, stream);
                 else
-                    matmul_impl(g, dtype, r.input, cols, r.rows, direction, r.output, r.rows * outCols, 0, 0,
+                    matmul_impl(g, dtype, r.input, cols, r.rows, direction, r.output, r.rows * outCols, 0, byIndiv,
                                 nullptr, GRGX_INIT_ZERO, nullptr, (flags & ~GRGX_FLAG_SYNC) | GRGX_FLAG_OVERWRITE,
                                 stream);
                 i = j;
@@ -123,7 +132,7 @@ void matmul_batch_impl(grgx_graph* g, const grgx_request* reqs, uint64_t n, uint
                                               static_cast<long long>(cols), red + row, s);
                 row += r.rows;
             }
-            matmul_impl(g, dtype, in, cols, rowsTotal, direction, out, rowsTotal * outCols, 0, 0, nullptr,
+            matmul_impl(g, dtype, in, cols, rowsTotal, direction, out, rowsTotal * outCols, 0, byIndiv, nullptr,
                         GRGX_INIT_ZERO, nullptr, passFlags, stream);
             row = 0;
             for (size_t k = i; k < j; k++) {

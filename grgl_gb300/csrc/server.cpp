@@ -102,8 +102,9 @@ struct grgx_server {
                     rows = head->r.rows;
                     for (size_t i = 1; i < pending.size(); i++) {
                         const Req& q = *pending[i];
+                        const bool sameFold = ((q.r.options ^ head->r.options) & GRGX_REQUEST_BY_INDIVIDUAL) == 0;
                         if (q.graph == head->graph && q.r.direction == head->r.direction && q.r.dtype == head->r.dtype &&
-                            rows + q.r.rows <= width) {
+                            sameFold && rows + q.r.rows <= width) {
                             take.push_back(i);
                             rows += q.r.rows;
                         }
@@ -244,7 +245,8 @@ grgx_status grgx_server_submit(grgx_server* s, uint32_t graph_id, const grgx_req
                    GRGX_ERR_API_MISUSE, "Invalid traversal direction");
         GRGX_CHECK(request->dtype >= GRGX_F64 && request->dtype <= GRGX_BOOL, GRGX_ERR_API_MISUSE,
                    "Unsupported dtype");
-        GRGX_CHECK((request->options & ~GRGX_REQUEST_STANDARDIZED) == 0, GRGX_ERR_API_MISUSE,
+        GRGX_CHECK((request->options & ~(GRGX_REQUEST_STANDARDIZED | GRGX_REQUEST_BY_INDIVIDUAL)) == 0,
+                   GRGX_ERR_API_MISUSE,
                    "Unknown request options");
         GRGX_CHECK(!(request->options & GRGX_REQUEST_STANDARDIZED) || request->dtype == GRGX_F32 ||
                        request->dtype == GRGX_F64,

@@ -175,13 +175,15 @@ grgx_status grgx_matmul_gram(grgx_graph* g, grgx_dtype dtype, const void* input,
                              uint64_t input_rows, grgx_direction first, void* output, uint64_t output_size,
                              int standardized, uint32_t flags, void* stream);
 
-/* One request of a batch or of the server: the plain product (no init, miss, emit_all_nodes or
- * by_individual) of `rows` x cols `input` in `direction`, written to `output` (rows x out_cols,
- * overwritten).  Host or device memory as the call's flags say.  With
+/* One request of a batch or of the server: the product (no init, miss or emit_all_nodes) of
+ * `rows` x cols `input` in `direction`, written to `output` (rows x out_cols, overwritten).  Host or device memory as the call's flags say.  With
  * GRGX_REQUEST_STANDARDIZED in `options` the product is the one grgx_matmul_standardized
  * computes (float32/float64 only); it still shares the traversal with the plain requests
  * stacked beside it. */
 #define GRGX_REQUEST_STANDARDIZED 0x1u
+/* by_individual (grg.h:1341-1517): UP input / DOWN output columns are individuals, the samples'
+ * values folded by ploidy; requests with and without it run in separate traversals. */
+#define GRGX_REQUEST_BY_INDIVIDUAL 0x2u
 typedef struct {
     grgx_dtype dtype;
     grgx_direction direction;

@@ -113,3 +113,34 @@ def test_server_memory_admission(gx, graphs):
         for t in ts:
             out, _ = srv.result(t, timeout=60)
             assert np.array_equal(out, gx.matmul(g, small, UP))
+
+
+def test_by_individual_requests_batched_and_served(gx, graphs):
+    """Requests folded by individual share traversals with each other (never with per-haplotype
+    ones) and equal matmul(..., by_individual=True)."""
+    g = graphs[0]
+    rng = np.random.default_rng(12)
+    reqs = []
+    for i in range(10):
+        d = UP if i % 2 else DOWN
+        byi = i % 3 != 0
+        dt = [np.int32, np.float64][i % 2]
+        cols = (g.num_individuals if byi else g.num_samples) if d == UP else g.num_mutations
+        reqs.append((_rand(rng, dt, (int(rng.integers(1, 7)), cols)), d, False, byi))
+    outs = gx.matmul_batch(g, reqs)
+    for (V, d, _, byi), out in zip(reqs, outs):
+        ref = gx.matmul(g, V, d, by_individual=byi)
+        if V.dtype.kind == "f":
+            scale = np.abs(gx.matmul(g, np.abs(V), d, by_individual=byi))
+            assert_matches(out, ref, scale, rtol=1e-12)
+        else:
+            assert_matches(out, ref)
+    with gx.Server(workers=2) as srv:
+        gid = srv.add_graph(g)
+        ts = [srv.submit(gid, V, d, by_individual=byi) for V, d, _, byi in reqs]
+        for (V, d, _, byi), t in zip(reqs, ts):
+            out, _ = srv.result(t, timeout=120)
+            if V.dtype.kind != "f":
+                assert np.array_equal(out, gx.matmul(g, V, d, by_individual=byi))
+    with pytest.raises(RuntimeError, match="per haplotype"):
+        gx.matmul_batch(g, [(np.ones((1, g.num_samples), dtype=np.float32), UP, True, True)])
