@@ -71,9 +71,12 @@ struct grgx_server {
     // storage (8 bytes), the stacked input/output, plus a quarter for partials and the pool.
     uint64_t estimate(const grgx::HostGraph& h, int dtype, uint64_t rows) const {
         const uint64_t es = elem(dtype);
+        // node values and the DOWN input rows (8 bytes an element at most), the split-form UP
+        // state (16 bytes an element at most), heavy-row partials (a quarter more), and the I/O
         const uint64_t valueBytes = (h.num_nodes + h.num_mutations) * rows * 8;
+        const uint64_t stateBytes = h.num_nodes * rows * 16;
         const uint64_t ioBytes = rows * (h.num_samples + h.num_mutations) * es * 2;
-        return valueBytes + valueBytes / 4 + ioBytes;
+        return valueBytes + valueBytes / 4 + stateBytes + ioBytes;
     }
 
     void worker_main() {
