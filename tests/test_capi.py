@@ -215,3 +215,22 @@ def test_saved_file_reads_in_the_reference(gx, tmp_path):
     V, W = rng.standard_normal((3, 500)), rng.standard_normal((2, 3000))
     assert np.array_equal(pygrgl.matmul(r, V, pygrgl.TraversalDirection.UP), oracle.matmul(og, V, UP))
     assert np.array_equal(pygrgl.matmul(r, W, pygrgl.TraversalDirection.DOWN), oracle.matmul(og, W, DOWN))
+
+
+def test_header_is_plain_c(tmp_path):
+    """include/grgx.h is a C header (C99, no C++ or CUDA types): a C program that includes it
+    and names every entry point compiles."""
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    header = (ROOT / "include" / "grgx.h").read_text()
+    names = sorted(set(re.findall(r"\b(grgx_[a-z0-9_]+)\s*\(", header)))
+    src = tmp_path / "abi.c"
+    src.write_text('#include "grgx.h"\ntypedef void (*entry)(void);\nentry table[] = {' +
+                   ", ".join(f"(entry){n}" for n in names) + "};\n")
+    res = subprocess.run([cc, "-std=c99", "-Wall", "-Werror", "-pedantic", "-fsyntax-only",
+                          f"-I{ROOT / 'include'}", str(src)], capture_output=True, text=True)
+    assert res.returncode == 0, res.stderr
