@@ -51,7 +51,7 @@ def parse_args():
                     help="print per-matmul device times (3 calls each, CUDA events) instead of the JSON line")
     ap.add_argument("--no-serve", action="store_true", help="skip the batched and served measurements")
     ap.add_argument("--batch-requests", type=int, default=256, help="requests in the batched measurement")
-    ap.add_argument("--serve-rates", default="50,200,1000,2000", help="Poisson arrival rates (requests/s)")
+    ap.add_argument("--serve-rates", default="50,200,500,1000,2000", help="Poisson arrival rates (requests/s)")
     ap.add_argument("--serve-seconds", type=float, default=4.0, help="longest arrival window of a served run")
     ap.add_argument("--serve-requests", type=int, default=96, help="most arrivals in a served run")
     ap.add_argument("--no-large", action="store_true", help="skip the large-graph measurement")
@@ -286,25 +286,42 @@ def served(gx, graphs, rate, seconds, max_requests, rng):
         th = threading.Thread(target=producer)
         t0 = time.perf_counter()
         th.start()
-        batches = []
+        batches, kept = [], {}
         for i in range(len(arrivals)):
             while tickets[i] is None:
                 time.sleep(0.0005)
-            _, st = srv.result(tickets[i], timeout=600)
+            out, st = srv.result(tickets[i], timeout=600)
+            if i % 4 == 0:
+                kept[i] = out  # every fourth result is checked against the same request alone
             lat.append(st["latency_s"])
             batches.append(st["batch_requests"])
         th.join()
         t_served = time.perf_counter() - t0
     t0 = time.perf_counter()
-    for _, gi, d, V in arrivals:
-        gx.matmul(graphs[gi], V, d)
+    alone = {}
+    for i, (_, gi, d, V) in enumerate(arrivals):
+        r = gx.matmul(graphs[gi], V, d)
+        if i in kept:
+            alone[i] = r
     t_plain = time.perf_counter() - t0
+    # in the mix vs alone: integer results bit-exact; float32 sums may differ in their last bits
+    # because a stacked call can run a different launch shape (another order of the additions)
+    int_exact, f32_diff = True, 0.0
+    for i, a in alone.items():
+        b = kept[i]
+        if a.dtype == np.int32:
+            int_exact &= bool(np.array_equal(a, b))
+        else:
+            scale = max(float(np.max(np.abs(a))), 1e-30)
+            f32_diff = max(f32_diff, float(np.max(np.abs(a.astype(np.float64) - b))) / scale)
     lat_ms = np.array(lat) * 1e3
     return {"arrival_rate_per_s": rate, "requests": len(arrivals),
             "arrival_window_s": arrivals[-1][0] if arrivals else 0.0,
             "p50_ms": float(np.percentile(lat_ms, 50)), "p99_ms": float(np.percentile(lat_ms, 99)),
             "served_edgeK_per_s": units / t_served, "plain_sequential_edgeK_per_s": units / t_plain,
-            "mean_batch_requests": float(np.mean(batches))}
+            "mean_batch_requests": float(np.mean(batches)),
+            "mix_vs_alone": {"checked": len(alone), "int32_bit_exact": int_exact,
+                             "float32_max_diff_rel_to_max": f32_diff}}
 
 
 def cold_start(gx, torch, g):
@@ -509,13 +526,17 @@ def main():
     if not args.no_autotune:
         gx.autotune_clear()
         t0 = time.perf_counter()
-        levels_tuned = 0
+        levels_tuned, up_form = 0, {}
         for dt, K, d in dict.fromkeys(combos):
-            levels_tuned += sum(1 for ln in gx.autotune(g, dt, K, d).splitlines() if " rows " in ln)
+            rep = gx.autotune(g, dt, K, d)
+            levels_tuned += sum(1 for ln in rep.splitlines() if " rows " in ln)
+            for ln in rep.splitlines():
+                if ln.startswith("UP runs"):
+                    up_form[f"{np.dtype(dt).name}:{K}"] = "split" if "split form" in ln else "unsplit"
         torch.cuda.synchronize()
         table = gx.autotune_table()
         tune = {"seconds": time.perf_counter() - t0, "levels_tuned": levels_tuned,
-                "table_entries": len(table.strip().splitlines())}
+                "table_entries": len(table.strip().splitlines()), "up_form": up_form}
         print("autotune table (kind stride rows_log2 degree_log2 g tiles variant):\n" + table, file=sys.stderr)
 
     # warm-up

@@ -121,11 +121,13 @@ __global__ void load_rows_df_kernel(const double* __restrict__ src, long long K,
     for (int j = ty; j < 32; j += 8) {
         const long long r = i0 + j, k = k0 + tx;
         if (r < R && k < stride) {
-            DF* d = dst + r * stride + k;
+            const long long e = r * stride + k;
             if (add) {
-                if (k < K) *d = AddF64S::split(AddF64S::value(*d) + AddF64S::value(tile[tx][j]));
+                if (k < K)
+                    df_put(dst, e, stride,
+                           AddF64S::split(AddF64S::value(df_get(dst, e, stride)) + AddF64S::value(tile[tx][j])));
             } else {
-                *d = tile[tx][j];
+                df_put(dst, e, stride, tile[tx][j]);
             }
         }
     }
@@ -145,10 +147,10 @@ __global__ void store_cols_df_kernel(const DF* __restrict__ vals, long long stri
         double v = 0.0;
         if (c < C && k < K) {
             if (mode == MAP_FOLD) {
-                for (long long p = 0; p < fold; p++) v += AddF64S::value(vals[(c * fold + p) * stride + k]);
+                for (long long p = 0; p < fold; p++) v += AddF64S::value(df_get(vals, (c * fold + p) * stride + k, stride));
             } else {
                 const long long node = (mode == MAP_TABLE) ? (long long)tab[c] : c;
-                if (node != (long long)kInvalid) v = AddF64S::value(vals[node * stride + k]);
+                if (node != (long long)kInvalid) v = AddF64S::value(df_get(vals, node * stride + k, stride));
             }
             v *= pow2(row_exp(rowmax, k));
         }
@@ -173,7 +175,7 @@ __global__ void init_vector_df_kernel(const double* __restrict__ init, long long
     for (long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x; x < total;
          x += (long long)gridDim.x * blockDim.x) {
         const long long k = x % stride;
-        vals[x] = (k < K) ? split_scaled(init[k], row_exp(rowmax, k)) : DF{0.f, 0.f};
+        df_put(vals, x, stride, (k < K) ? split_scaled(init[k], row_exp(rowmax, k)) : DF{0.f, 0.f});
     }
 }
 
@@ -184,7 +186,7 @@ __global__ void init_xtx_df_kernel(const uint32_t* __restrict__ xtx, long long K
     for (long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x; x < total;
          x += (long long)gridDim.x * blockDim.x) {
         const long long k = x % stride, v = x / stride;
-        vals[x] = (k < K) ? split_scaled(static_cast<double>(xtx[v]), row_exp(rowmax, k)) : DF{0.f, 0.f};
+        df_put(vals, x, stride, (k < K) ? split_scaled(static_cast<double>(xtx[v]), row_exp(rowmax, k)) : DF{0.f, 0.f});
     }
 }
 

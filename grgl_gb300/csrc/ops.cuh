@@ -141,6 +141,25 @@ struct alignas(8) DF {
     float hi, lo;
 };
 
+// Storage of float-pair node values.  With an even row stride (rows of two or more columns)
+// columns 2j and 2j+1 of a row are stored as (hi_2j, hi_2j+1, lo_2j, lo_2j+1): a 16-byte load
+// then gives the two high parts and the two low parts as register pairs, the operands of the
+// packed float2 arithmetic, with no moves between them.  With stride 1 a value is (hi, lo).
+__device__ __forceinline__ DF df_get(const DF* base, long long e, long long stride) {
+    if (stride & 1) return base[e];
+    const float* f = reinterpret_cast<const float*>(base) + 4 * (e >> 1) + (e & 1);
+    return {f[0], f[2]};
+}
+__device__ __forceinline__ void df_put(DF* base, long long e, long long stride, DF v) {
+    if (stride & 1) {
+        base[e] = v;
+        return;
+    }
+    float* f = reinterpret_cast<float*>(base) + 4 * (e >> 1) + (e & 1);
+    f[0] = v.hi;
+    f[2] = v.lo;
+}
+
 struct F64Run {
     double acc;
     float hi, lo;

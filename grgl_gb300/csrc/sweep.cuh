@@ -64,14 +64,21 @@ template <> struct Vec<float, 4> { static __device__ __forceinline__ void ld(con
 template <> struct Vec<double, 1> { static __device__ __forceinline__ void ld(const double* p, double* v) { v[0] = __ldg(p); } static __device__ __forceinline__ void st(double* p, const double* v) { p[0] = v[0]; } };
 template <> struct Vec<double, 2> { static __device__ __forceinline__ void ld(const double* p, double* v) { double2 t = __ldg(reinterpret_cast<const double2*>(p)); v[0] = t.x; v[1] = t.y; } static __device__ __forceinline__ void st(double* p, const double* v) { *reinterpret_cast<double2*>(p) = make_double2(v[0], v[1]); } };
 template <> struct Vec<DF, 1> { static __device__ __forceinline__ void ld(const DF* p, DF* v) { float2 t = __ldg(reinterpret_cast<const float2*>(p)); v[0] = {t.x, t.y}; } static __device__ __forceinline__ void st(DF* p, const DF* v) { *reinterpret_cast<float2*>(p) = make_float2(v[0].hi, v[0].lo); } };
-template <> struct Vec<DF, 2> { static __device__ __forceinline__ void ld(const DF* p, DF* v) { float4 t = __ldg(reinterpret_cast<const float4*>(p)); v[0] = {t.x, t.y}; v[1] = {t.z, t.w}; } static __device__ __forceinline__ void st(DF* p, const DF* v) { *reinterpret_cast<float4*>(p) = make_float4(v[0].hi, v[0].lo, v[1].hi, v[1].lo); } };
+// two columns of float pairs, stored (hi, hi, lo, lo): see df_get
+template <> struct Vec<DF, 2> { static __device__ __forceinline__ void ld(const DF* p, DF* v) { float4 t = __ldg(reinterpret_cast<const float4*>(p)); v[0] = {t.x, t.z}; v[1] = {t.y, t.w}; } static __device__ __forceinline__ void st(DF* p, const DF* v) { *reinterpret_cast<float4*>(p) = make_float4(v[0].hi, v[1].hi, v[0].lo, v[1].lo); } };
 template <> struct Vec<unsigned long long, 1> { static __device__ __forceinline__ void ld(const unsigned long long* p, unsigned long long* v) { v[0] = __ldg(p); } static __device__ __forceinline__ void st(unsigned long long* p, const unsigned long long* v) { p[0] = v[0]; } };
 template <> struct Vec<unsigned long long, 2> { static __device__ __forceinline__ void ld(const unsigned long long* p, unsigned long long* v) { ulonglong2 t = __ldg(reinterpret_cast<const ulonglong2*>(p)); v[0] = t.x; v[1] = t.y; } static __device__ __forceinline__ void st(unsigned long long* p, const unsigned long long* v) { *reinterpret_cast<ulonglong2*>(p) = make_ulonglong2(v[0], v[1]); } };
 
 // Plain (coherent) load of the current destination value, for read-modify-write.
 template <typename S, int VW> __device__ __forceinline__ void ld_plain(const S* p, S* v) {
+    if constexpr (std::is_same<S, DF>::value && VW == 2) {
+        const float4 t = *reinterpret_cast<const float4*>(p);
+        v[0] = {t.x, t.z};
+        v[1] = {t.y, t.w};
+    } else {
 #pragma unroll
-    for (int i = 0; i < VW; i++) v[i] = p[i];
+        for (int i = 0; i < VW; i++) v[i] = p[i];
+    }
 }
 
 // Sum of a lane's accumulator over the 32/G groups of the warp (every group gets the result).

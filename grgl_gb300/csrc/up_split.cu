@@ -23,6 +23,7 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "device_plan.h"
@@ -104,9 +105,14 @@ __global__ void state_finish_kernel(const typename Op::A* __restrict__ state, ty
     for (long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x; x < total;
          x += (long long)gridDim.x * blockDim.x) {
         const long long node = nodes[x / stride], col = x % stride;
-        typename Op::S* d = vals + node * stride + col;
         const typename Op::A a = state[(node - base) * stride + col];
-        *d = rmw ? Op::finish_onto(*d, a) : Op::finish(a);
+        if constexpr (std::is_same<typename Op::S, DF>::value) {
+            const long long e = node * stride + col;
+            df_put(vals, e, stride, rmw ? Op::finish_onto(df_get(vals, e, stride), a) : Op::finish(a));
+        } else {
+            typename Op::S* d = vals + node * stride + col;
+            *d = rmw ? Op::finish_onto(*d, a) : Op::finish(a);
+        }
     }
 }
 
