@@ -641,7 +641,10 @@ def main():
                                     "K~U{1..128}, UP/DOWN 50/50, float32 compensated, half N(0,1) and half "
                                     "standardized inputs", std_every=2, err_sample=8),
                    batched_vs_plain(gx, torch, g, stats["edges"], rng2, nb, 8,
-                                    "K~U{1..8}, UP/DOWN 50/50, float32 compensated, N(0,1) inputs")]
+                                    "K~U{1..8}, UP/DOWN 50/50, float32 compensated, N(0,1) inputs"),
+                   batched_vs_plain(gx, torch, g, stats["edges"], rng2, nb, 1,
+                                    "K=1 (single-vector requests, the dot_product pattern), UP/DOWN 50/50, float32 "
+                                    "compensated, N(0,1) inputs")]
         g2 = gx.window_tree_grg(max(2, args.samples // 4), max(1, args.mutations * 3 // 10), seed=args.seed + 1)
         g2.upload()
         serve = {"graphs": [graph_stats(x) for x in (g, g2)],
