@@ -686,7 +686,8 @@ def main():
             "gpu_launches": launches,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "steps": None if args.no_e2e else e2e_steps, "statistic": "median step",
-                    "mean_value": None if args.no_e2e else e2e_mean},
+                    "mean_value": None if args.no_e2e else e2e_mean,
+                    "step_ms": None if args.no_e2e else [round(x * 1e3, 1) for x in e2e_times]},
             "cpu_baseline": cpu,
             "batched_vs_plain": batched,
             "served": serve,
