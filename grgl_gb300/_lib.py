@@ -14,6 +14,7 @@ LIB_PATH = Path(__file__).resolve().parent / "libgrgx.so"
 OK, ERR_API_MISUSE, ERR_CUDA, ERR_OOM, ERR_BAD_FILE, ERR_UNSUPPORTED, ERR_NO_DEVICE, ERR_TIMEOUT = range(8)
 FLAG_DEVICE_POINTERS, FLAG_F32_PLAIN, FLAG_SYNC, FLAG_OVERWRITE, FLAG_F64_NATIVE = 0x1, 0x2, 0x4, 0x8, 0x10
 FLAG_NO_GRAPH = 0x20
+FLAG_ASYNC = 0x40
 REQUEST_STANDARDIZED = 0x1
 REQUEST_BY_INDIVIDUAL = 0x2
 NOALLOC_SCRATCH_BYTES = 64 << 20  # GRGX_NOALLOC_SCRATCH_BYTES

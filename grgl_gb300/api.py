@@ -269,6 +269,16 @@ def matmul(grg: GRG, input, direction, emit_all_nodes: bool = False, by_individu
     if _is_torch_cuda(input):
         return _matmul_device(grg, input, direction, emit_all_nodes, by_individual, init, miss,
                               _flags(f32_compensated, f64_native))
+    out, keep = _matmul_host(grg, input, direction, emit_all_nodes, by_individual, init, miss,
+                             _flags(f32_compensated, f64_native), None)
+    _finish_miss(miss, keep[2])
+    return out
+
+
+def _matmul_host(grg, input, direction, emit_all, by_indiv, init, miss, extra_flags, stream):
+    """The numpy form of matmul: validation as in dispatchMult (_grgl.cpp:108-183), then one
+    grgx_matmul on host buffers.  Returns the output and the buffers the call reads or writes
+    (input, init, miss as passed to the library), which an asynchronous call keeps alive."""
     direction = TraversalDirection(int(direction))
     if not isinstance(input, np.ndarray):
         raise RuntimeError(f"Unsupported numpy dtype: {np.asarray(input).dtype}")
@@ -278,19 +288,74 @@ def matmul(grg: GRG, input, direction, emit_all_nodes: bool = False, by_individu
     _check(rows != 0 and cols != 0, "matmul() requires non-zero dimensions.")
     _check(arr.dtype in _DTYPE_CODES, f"Unsupported numpy dtype: {arr.dtype}")
     code = _DTYPE_CODES[arr.dtype]
-    nsamp = grg.num_individuals if by_individual else grg.num_samples
-    out_cols = grg.num_nodes if emit_all_nodes else (nsamp if direction == DOWN else grg.num_mutations)
+    nsamp = grg.num_individuals if by_indiv else grg.num_samples
+    out_cols = grg.num_nodes if emit_all else (nsamp if direction == DOWN else grg.num_mutations)
     init_kind, init_arr = _parse_init(grg, init, arr.dtype, rows, code == 10)
-    miss_arr = _parse_miss(miss, arr.dtype, rows, cols, out_cols, direction, emit_all_nodes)
+    miss_arr = _parse_miss(miss, arr.dtype, rows, cols, out_cols, direction, emit_all)
     out = _host_empty((rows, out_cols), arr.dtype)
-    flags = _lib.FLAG_OVERWRITE | _flags(f32_compensated, f64_native)
+    flags = _lib.FLAG_OVERWRITE | extra_flags
     _lib.check(_lib.lib().grgx_matmul(grg._h, code, arr.ctypes.data, cols, rows, int(direction), out.ctypes.data,
-                                      out.size, int(bool(emit_all_nodes)), int(bool(by_individual)),
+                                      out.size, int(bool(emit_all)), int(bool(by_indiv)),
                                       init_arr.ctypes.data if init_arr is not None else None, init_kind,
-                                      miss_arr.ctypes.data if miss_arr is not None else None, flags, None))
+                                      miss_arr.ctypes.data if miss_arr is not None else None, flags, stream))
+    return out, (arr, init_arr, miss_arr)
+
+
+def _finish_miss(miss, miss_arr):
+    """UP writes `miss` in place: copy back when the library worked on a converted copy."""
     if miss_arr is not None and miss_arr is not miss:
         miss[...] = miss_arr
-    return out
+
+
+class PendingMatmul:
+    """A matmul on host buffers queued on a CUDA stream by matmul_async.  result() waits for the
+    stream to reach the end of the call and returns the output array; until then the output
+    (and an UP `miss`) are being written and the buffers passed to the call stay referenced."""
+
+    def __init__(self, out, miss, keep, event):
+        self._out, self._miss, self._keep, self._event = out, miss, keep, event
+
+    def done(self) -> bool:
+        """True once the call has finished on the device (result() will not wait)."""
+        return self._event.query()
+
+    def result(self):
+        if self._keep is not None:
+            self._event.synchronize()
+            _finish_miss(self._miss, self._keep[2])
+            self._keep = None
+        return self._out
+
+
+def matmul_async(grg: GRG, input, direction, emit_all_nodes: bool = False, by_individual: bool = False,
+                 init=None, miss=None, *, stream=None, f32_compensated: bool = True,
+                 f64_native: bool = False) -> PendingMatmul:
+    """matmul on numpy buffers without waiting for it (no counterpart in the reference).
+
+    The copy of the input to the device, the product and the copy of the result back are
+    queued on `stream` (a torch.cuda.Stream; default the current stream) and the call returns a
+    PendingMatmul at once; its result() returns the same array matmul would.  With inputs in
+    page-locked memory (host_empty), calls queued on two streams overlap one call's copies with
+    the other's product.  The arguments, checks and messages are those of matmul.
+    """
+    import torch
+
+    if _is_torch_cuda(input):
+        raise RuntimeError("matmul_async takes numpy arrays; device tensors are asynchronous with matmul already")
+    if stream is None:
+        stream = torch.cuda.current_stream()
+    out, keep = _matmul_host(grg, input, direction, emit_all_nodes, by_individual, init, miss,
+                             _flags(f32_compensated, f64_native) | _lib.FLAG_ASYNC, stream.cuda_stream)
+    event = torch.cuda.Event()
+    event.record(stream)
+    return PendingMatmul(out, miss, keep, event)
+
+
+def host_empty(shape, dtype):
+    """An uninitialised numpy array in page-locked (pinned, pooled) host memory when it is 4 MiB
+    or larger, else in plain numpy memory: inputs in it reach the device at the link's full
+    speed and let matmul_async overlap their copies with other work."""
+    return _host_empty(shape, dtype)
 
 
 def _parse_init(grg, init, dtype, rows, is_bool):

@@ -79,6 +79,11 @@ void setup_pool_once(int device) {
     GRGX_CUDA(cudaDeviceGetDefaultMemPool(&pool, device));
     uint64_t threshold = UINT64_MAX;
     GRGX_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &threshold));
+    // Calls on different streams must not be chained through the pool: a block freed by a call
+    // still running on one stream is not handed to another stream's call (which would make it
+    // wait for the first), only blocks whose free has completed are.
+    int noChain = 0;
+    GRGX_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolReuseAllowInternalDependencies, &noChain));
     done.push_back(device);
 }
 
@@ -634,7 +639,8 @@ void matmul_direct(grgx_graph* g, int dtype, const void* input, uint64_t in_cols
     } else {
         t_last.launches = launches;
     }
-    if (!devPtrs || (flags & GRGX_FLAG_SYNC)) GRGX_CUDA(cudaStreamSynchronize(s));
+    const bool hostWait = !devPtrs && !(flags & GRGX_FLAG_ASYNC);
+    if (hostWait || (flags & GRGX_FLAG_SYNC)) GRGX_CUDA(cudaStreamSynchronize(s));
 }
 
 // ---- captured CUDA graphs of whole calls (small graphs) ----------------------------------------
@@ -757,7 +763,9 @@ void matmul_impl(grgx_graph* g, int dtype, const void* input, uint64_t in_cols, 
     std::lock_guard<std::mutex> lk(e->mu);
     const cudaMemcpyKind in = devPtrs ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
     const cudaMemcpyKind outk = devPtrs ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
-    if (devPtrs) {
+    // ordered after the caller's stream (device buffers, or host buffers queued asynchronously)
+    const bool onUser = devPtrs || (flags & GRGX_FLAG_ASYNC);
+    if (onUser) {
         GRGX_CUDA(cudaEventRecord(e->ready, user));
         GRGX_CUDA(cudaStreamWaitEvent(e->stream, e->ready, 0));
     }
@@ -769,7 +777,7 @@ void matmul_impl(grgx_graph* g, int dtype, const void* input, uint64_t in_cols, 
     GRGX_CUDA(cudaMemcpyAsync(output, e->out, e->outBytes, outk, e->stream));
     if (e->missBytes && direction == GRGX_DIRECTION_UP)
         GRGX_CUDA(cudaMemcpyAsync(miss, e->miss, e->missBytes, outk, e->stream));
-    if (devPtrs) {
+    if (onUser) {
         GRGX_CUDA(cudaEventRecord(e->done, e->stream));
         GRGX_CUDA(cudaStreamWaitEvent(user, e->done, 0));
         if (flags & GRGX_FLAG_SYNC) GRGX_CUDA(cudaStreamSynchronize(user));

@@ -62,6 +62,7 @@ typedef enum { GRGX_INIT_ZERO = 0, GRGX_INIT_VECTOR = 1, GRGX_INIT_MATRIX = 2, G
 #define GRGX_FLAG_OVERWRITE 0x8u       /* write the output instead of adding to it */
 #define GRGX_FLAG_F64_NATIVE 0x10u     /* f64: accumulate on the FP64 pipe instead of as scaled float pairs */
 #define GRGX_FLAG_NO_GRAPH 0x20u       /* never replay a captured CUDA graph for this call */
+#define GRGX_FLAG_ASYNC 0x40u          /* grgx_matmul with host pointers: return once queued (below) */
 
 typedef struct {
     uint64_t num_nodes;
@@ -140,8 +141,12 @@ grgx_status grgx_graph_upload(grgx_graph* g);
  *   stream      cudaStream_t (NULL = legacy default stream)
  * With GRGX_FLAG_DEVICE_POINTERS the buffers are device pointers and the call is
  * asynchronous on `stream`; otherwise they are host pointers and the call returns when the
- * output (and miss) have been written back.  Validation and messages follow
- * validateMatMulInputs (internal_mult.h:130-158).
+ * output (and miss) have been written back -- unless GRGX_FLAG_ASYNC is set: then the copies
+ * in and out are queued on `stream` with the product and the call returns at once; the caller
+ * keeps every host buffer alive and synchronizes `stream` before reading the output.  With
+ * page-locked host buffers (grgx_host_alloc) the copies of one call then overlap the products
+ * of calls queued on other streams.  Validation and messages follow validateMatMulInputs
+ * (internal_mult.h:130-158).
  * On small graphs (at most 2^25 edges) the first call of each shape (dtype, K, direction,
  * options, stream) captures the whole call into a CUDA graph, which later calls of that shape
  * replay through staging buffers -- one launch instead of one per level.  The first call of a
