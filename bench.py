@@ -45,6 +45,8 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline sample budget")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end pass")
+    ap.add_argument("--e2e-streams", type=int, default=4,
+                    help="CUDA streams the end-to-end pass spreads the step's calls over")
     ap.add_argument("--only", default=None,
                     help="restrict the step to dtype:K:dir entries, e.g. float32:64:UP,int32:1:DOWN")
     ap.add_argument("--breakdown", action="store_true",
@@ -614,12 +616,12 @@ def main():
             P = gx.host_empty(V.shape, V.dtype)
             P[...] = V
             pinned_inputs.append(P)
-        streams = [torch.cuda.Stream(), torch.cuda.Stream()]
+        streams = [torch.cuda.Stream() for _ in range(max(1, args.e2e_streams))]
 
         def step_async(inputs):
-            # the step's calls alternate between two streams, so one call's copies overlap the
-            # other stream's product; every result is read back before the step ends
-            pend = [gx.matmul_async(g, V, d, stream=streams[i % 2])
+            # the step's calls go round-robin over the streams, so one call's copies overlap the
+            # other streams' products; every result is read back before the step ends
+            pend = [gx.matmul_async(g, V, d, stream=streams[i % len(streams)])
                     for i, ((_, _, d), V) in enumerate(zip(combos, inputs))]
             for p in pend:
                 p.result()
@@ -706,7 +708,7 @@ def main():
                     "mean_value": None if args.no_e2e else e2e_mean,
                     "step_ms": None if args.no_e2e else [round(x * 1e3, 1) for x in e2e_times],
                     "api": "grgl_gb300.matmul_async on numpy inputs in pinned memory (C ABI grgx_matmul, host "
-                           "pointers, GRGX_FLAG_ASYNC), calls alternating between two CUDA streams",
+                           f"pointers, GRGX_FLAG_ASYNC), calls round-robin over {args.e2e_streams} CUDA streams",
                     "one_call_at_a_time": e2e_sync},
             "cpu_baseline": cpu,
             "batched_vs_plain": batched,
