@@ -384,6 +384,53 @@ extern "C" grgx_status grgx_graph_upload_host_plan(grgx_graph* g) {
     });
 }
 
+// Test hook (not part of the public header): one array of the plan the host builder lays out
+// for `g` (plan.cpp: the renumbering, the level ranges, the UP/DOWN/seed rows, offsets and
+// chunks -- the stages the device builder shares), so that its invariants can be checked
+// without a GPU.  Names: "level_begin", "old2new", "new2old", "mut_new", "miss_new",
+// "down_row_of", and "<csr>.<field>" for csr in up/down/seed/miss and field in rows/off/adj/
+// chunks/heavy/level_chunk_begin/level_chunk_end.  The arrays stay valid until the graph is
+// destroyed.
+extern "C" grgx_status grgx_debug_host_plan(grgx_graph* g, const char* name, const void** data,
+                                            uint64_t* bytes) {
+    return guarded([&] {
+        GRGX_CHECK(g && name && data && bytes, GRGX_ERR_API_MISUSE, "null argument");
+        {
+            std::lock_guard<std::mutex> lk(g->mu);
+            if (!g->inspect_plan) g->inspect_plan = grgx::build_plan(g->host_edges());
+        }
+        const grgx::HostPlan& p = *g->inspect_plan;
+        bool found = false;
+        auto put = [&](const auto& v) {
+            *data = v.data();
+            *bytes = static_cast<uint64_t>(v.size() * sizeof(v[0]));
+            found = true;
+        };
+        const std::string n(name);
+        if (n == "level_begin") put(p.level_begin);
+        else if (n == "old2new") put(p.old2new);
+        else if (n == "new2old") put(p.new2old);
+        else if (n == "mut_new") put(p.mut_new);
+        else if (n == "miss_new") put(p.miss_new);
+        else if (n == "down_row_of") put(p.down_row_of);
+        const std::pair<const char*, const grgx::PullCSR*> csrs[] = {
+            {"up.", &p.up}, {"down.", &p.down}, {"seed.", &p.seed}, {"miss.", &p.miss}};
+        for (const auto& c : csrs) {
+            if (n.rfind(c.first, 0) != 0) continue;
+            const std::string f = n.substr(std::string(c.first).size());
+            const grgx::PullCSR& P = *c.second;
+            if (f == "rows") put(P.rows);
+            else if (f == "off") put(P.off);
+            else if (f == "adj") put(P.adj);
+            else if (f == "chunks") put(P.chunks);
+            else if (f == "heavy") put(P.heavy);
+            else if (f == "level_chunk_begin") put(P.level_chunk_begin);
+            else if (f == "level_chunk_end") put(P.level_chunk_end);
+        }
+        GRGX_CHECK(found, GRGX_ERR_API_MISUSE, "unknown plan array: " + n);
+    });
+}
+
 // Test hook (not part of the public header): the block of height-0 ids used by split copies
 // built from now on (0 keeps it) and the height-0 row bytes above which UP runs in split form.
 extern "C" void grgx_debug_up_split(long long block, unsigned long long threshold_bytes) {

@@ -165,6 +165,7 @@ struct grgx_graph {
     }
     std::unique_ptr<grgx::HostGraph> host;
     std::unique_ptr<grgx::HostPlan> plan;
+    std::unique_ptr<grgx::HostPlan> inspect_plan;  // host-built plan kept for grgx_debug_host_plan
     std::unique_ptr<grgx::DevicePlan, grgx::DevicePlanDeleter> dev;
     std::unique_ptr<grgx::GraphCache, grgx::GraphCacheDeleter> graphs;  // destroyed before `dev`
     std::mutex mu;  // guards plan/dev creation
