@@ -24,6 +24,7 @@ void matmul_impl(grgx_graph* g, int dtype, const void* input, uint64_t in_cols, 
 void matmul_standardized_impl(grgx_graph* g, int dtype, const void* input, uint64_t in_cols, uint64_t rows,
                               int direction, void* output, uint64_t output_size, uint32_t flags, void* stream);
 DevicePlan* standardized_plan(grgx_graph* g, cudaStream_t s);
+cudaError_t pool_malloc(void** p, size_t bytes, cudaStream_t s);
 void standardized_prepare_down(int dtype, const DevicePlan* dp, void* V, long long K, long long M, double* c,
                                cudaStream_t s);
 void standardized_finish_down(int dtype, void* Y, const double* c, long long K, long long N, cudaStream_t s);
@@ -116,11 +117,11 @@ void matmul_batch_impl(grgx_graph* g, const grgx_request* reqs, uint64_t n, uint
             for (size_t k = i; k < j; k++) anyStd |= (reqs[idx[k]].options & GRGX_REQUEST_STANDARDIZED) != 0;
             DevicePlan* dp = anyStd ? standardized_plan(g, s) : nullptr;
             double* red = nullptr;
-            if (anyStd) BATCH_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&red), rowsTotal * sizeof(double), s));
+            if (anyStd) BATCH_CUDA(pool_malloc(reinterpret_cast<void**>(&red), rowsTotal * sizeof(double), s));
             void* in = nullptr;
             void* out = nullptr;
-            BATCH_CUDA(cudaMallocAsync(&in, rowsTotal * cols * es, s));
-            BATCH_CUDA(cudaMallocAsync(&out, rowsTotal * outCols * es, s));
+            BATCH_CUDA(pool_malloc(&in, rowsTotal * cols * es, s));
+            BATCH_CUDA(pool_malloc(&out, rowsTotal * outCols * es, s));
             uint64_t row = 0;
             for (size_t k = i; k < j; k++) {
                 const grgx_request& r = reqs[idx[k]];

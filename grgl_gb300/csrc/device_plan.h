@@ -124,4 +124,13 @@ void set_up_split_choice(grgx_graph* g, DevicePlan* dp, const Layout& L, bool sp
 // Builds (once) and returns the graph's plan on the current device.
 DevicePlan* ensure_device_plan(grgx_graph* g);
 
+// cudaMallocAsync from the device's stream-ordered pool.  The pool never makes a call wait for
+// a call on another stream, so under memory pressure the blocks such calls have freed can still
+// be in flight: then the device is drained once and the allocation retried (not inside a stream
+// capture, where the first error stands).
+cudaError_t pool_malloc(void** p, size_t bytes, cudaStream_t s);
+// Hands the memory the pool keeps cached between calls back to the device (after an ordinary
+// allocation ran out of memory).
+void trim_pool();
+
 }  // namespace grgx

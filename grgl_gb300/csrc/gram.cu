@@ -52,11 +52,11 @@ void matmul_gram_impl(grgx_graph* g, int dtype, const void* input, uint64_t in_c
     const uint32_t pass = (flags & (GRGX_FLAG_F32_PLAIN | GRGX_FLAG_F64_NATIVE)) | GRGX_FLAG_DEVICE_POINTERS |
                           GRGX_FLAG_OVERWRITE;
     void *dIn = const_cast<void*>(input), *dOut = output, *tmp = nullptr;
-    GRGX_CUDA(cudaMallocAsync(&tmp, rows * mid * es, s));
+    GRGX_CUDA(pool_malloc(&tmp, rows * mid * es, s));
     if (!dev) {
-        GRGX_CUDA(cudaMallocAsync(&dIn, rows * cols * es, s));
+        GRGX_CUDA(pool_malloc(&dIn, rows * cols * es, s));
         GRGX_CUDA(cudaMemcpyAsync(dIn, input, rows * cols * es, cudaMemcpyHostToDevice, s));
-        GRGX_CUDA(cudaMallocAsync(&dOut, rows * cols * es, s));
+        GRGX_CUDA(pool_malloc(&dOut, rows * cols * es, s));
     }
     const int second = up ? GRGX_DIRECTION_DOWN : GRGX_DIRECTION_UP;
     if (standardized) {

@@ -132,7 +132,7 @@ struct Scratch {
     void* get(size_t bytes) {
         if (bytes == 0) bytes = 16;
         void* p = nullptr;
-        GRGX_CUDA(cudaMallocAsync(&p, bytes, s));
+        GRGX_CUDA(pool_malloc(&p, bytes, s));
         ptrs.push_back(p);
         return p;
     }
@@ -280,7 +280,28 @@ uint32_t* device_plan_build(const HostGraph& hg, std::unique_ptr<HostPlan>& out)
 }
 }  // namespace
 
-DevicePlan* ensure_device_plan(grgx_graph* g) {
+cudaError_t pool_malloc(void** p, size_t bytes, cudaStream_t s) {
+    cudaError_t e = cudaMallocAsync(p, bytes, s);
+    if (e != cudaErrorMemoryAllocation) return e;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return e;
+    cudaGetLastError();
+    const cudaError_t se = cudaDeviceSynchronize();
+    if (se != cudaSuccess) return se;
+    return cudaMallocAsync(p, bytes, s);
+}
+
+void trim_pool() {
+    int device = 0;
+    cudaMemPool_t pool;
+    if (cudaGetDevice(&device) != cudaSuccess || cudaDeviceGetDefaultMemPool(&pool, device) != cudaSuccess) return;
+    cudaDeviceSynchronize();
+    cudaMemPoolTrimTo(pool, 0);
+    cudaGetLastError();
+}
+
+namespace {
+DevicePlan* ensure_device_plan_once(grgx_graph* g) {
     std::lock_guard<std::mutex> lk(g->mu);
     int device = 0;
     GRGX_CUDA(cudaGetDevice(&device));
@@ -327,6 +348,23 @@ DevicePlan* ensure_device_plan(grgx_graph* g) {
     g->dev = std::move(d);
     g->plan.reset();  // the device copy is authoritative; free the host copy
     return g->dev.get();
+}
+}  // namespace
+
+DevicePlan* ensure_device_plan(grgx_graph* g) {
+    try {
+        return ensure_device_plan_once(g);
+    } catch (const Error& e) {
+        if (e.code != GRGX_ERR_OUT_OF_MEMORY) throw;
+    }
+    // out of device memory: hand the memory the pool keeps between calls back to the device
+    // and build the plan once more from the start
+    {
+        std::lock_guard<std::mutex> lk(g->mu);
+        g->plan.reset();
+    }
+    trim_pool();
+    return ensure_device_plan_once(g);
 }
 
 uint64_t device_plan_bytes(const grgx_graph* g) { return g->dev ? g->dev->bytes : 0; }

@@ -108,8 +108,8 @@ void ensure_stats(grgx_graph* g, DevicePlan* dp, cudaStream_t s) {
     const HostGraph& h = *g->host;
     const long long N = static_cast<long long>(h.num_samples), M = static_cast<long long>(h.num_mutations);
     int *ones = nullptr, *counts = nullptr;
-    GRGX_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&ones), std::max<long long>(N, 1) * sizeof(int), s));
-    GRGX_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&counts), std::max<long long>(M, 1) * sizeof(int), s));
+    GRGX_CUDA(pool_malloc(reinterpret_cast<void**>(&ones), std::max<long long>(N, 1) * sizeof(int), s));
+    GRGX_CUDA(pool_malloc(reinterpret_cast<void**>(&counts), std::max<long long>(M, 1) * sizeof(int), s));
     fill_ones_kernel<<<grid_for(N), 256, 0, s>>>(ones, N);
     matmul_impl(g, GRGX_I32, ones, N, 1, GRGX_DIRECTION_UP, counts, M, 0, 0, nullptr, GRGX_INIT_ZERO, nullptr,
                 GRGX_FLAG_DEVICE_POINTERS | GRGX_FLAG_OVERWRITE, s);
@@ -134,18 +134,18 @@ void run(grgx_graph* g, DevicePlan* dp, int dtype, const T* in, long long K, int
     const uint32_t pass = (flags & (GRGX_FLAG_F32_PLAIN | GRGX_FLAG_F64_NATIVE)) | GRGX_FLAG_DEVICE_POINTERS |
                           GRGX_FLAG_OVERWRITE;
     double* red = nullptr;
-    GRGX_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&red), K * sizeof(double), s));
+    GRGX_CUDA(pool_malloc(reinterpret_cast<void**>(&red), K * sizeof(double), s));
     const unsigned rowBlocks = static_cast<unsigned>(std::min<long long>(K, 65535));
     if (direction == GRGX_DIRECTION_UP) {
         T* vx = nullptr;
-        GRGX_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&vx), K * M * sizeof(T), s));
+        GRGX_CUDA(pool_malloc(reinterpret_cast<void**>(&vx), K * M * sizeof(T), s));
         matmul_impl(g, dtype, in, N, K, GRGX_DIRECTION_UP, vx, K * M, 0, 0, nullptr, GRGX_INIT_ZERO, nullptr, pass, s);
         row_sum_kernel<T><<<rowBlocks, 256, 0, s>>>(in, K, N, red);
         up_finish_kernel<T><<<grid_for(K * M), 256, 0, s>>>(vx, red, dp->freq, dp->inv_sigma, K, M, out);
         GRGX_CUDA(cudaFreeAsync(vx, s));
     } else {
         T* w = nullptr;
-        GRGX_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&w), K * M * sizeof(T), s));
+        GRGX_CUDA(pool_malloc(reinterpret_cast<void**>(&w), K * M * sizeof(T), s));
         down_prepare_kernel<T><<<rowBlocks, 256, 0, s>>>(in, K, M, dp->freq, dp->inv_sigma, w, red);
         matmul_impl(g, dtype, w, M, K, GRGX_DIRECTION_DOWN, out, K * N, 0, 0, nullptr, GRGX_INIT_ZERO, nullptr, pass,
                     s);
@@ -229,10 +229,10 @@ void matmul_standardized_impl(grgx_graph* g, int dtype, const void* input, uint6
     void* dOut = output;
     if (!dev) {
         void* a = nullptr;
-        GRGX_CUDA(cudaMallocAsync(&a, rows * in_cols * es, s));
+        GRGX_CUDA(pool_malloc(&a, rows * in_cols * es, s));
         GRGX_CUDA(cudaMemcpyAsync(a, input, rows * in_cols * es, cudaMemcpyHostToDevice, s));
         dIn = a;
-        GRGX_CUDA(cudaMallocAsync(&dOut, rows * outCols * es, s));
+        GRGX_CUDA(pool_malloc(&dOut, rows * outCols * es, s));
     }
     if (dtype == GRGX_F64)
         run<double>(g, dp, dtype, static_cast<const double*>(dIn), static_cast<long long>(rows), direction,

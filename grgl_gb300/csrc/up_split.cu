@@ -313,10 +313,15 @@ bool up_split_possible(const DevicePlan* dp) {
 
 void ensure_up_split(grgx_graph* g, DevicePlan* dp) {
     std::lock_guard<std::mutex> lk(g->mu);
-    if (!dp->split_built) {
+    if (dp->split_built) return;
+    try {
         build_up_split(*dp);
-        dp->split_built = true;
+    } catch (const Error& e) {
+        if (e.code != GRGX_ERR_OUT_OF_MEMORY) throw;
+        trim_pool();  // the memory the pool keeps between calls goes back to the device
+        build_up_split(*dp);
     }
+    dp->split_built = true;
 }
 
 void set_up_split_choice(grgx_graph* g, DevicePlan* dp, const Layout& L, bool split) {
