@@ -42,7 +42,7 @@ def build(force: bool = False) -> Path:
     if not force and LIB_PATH.exists() and LIB_PATH.stat().st_mtime >= src.stat().st_mtime:
         return LIB_PATH
     tmp = LIB_PATH.with_suffix(".so.tmp")
-    subprocess.run(["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-ffp-contract=off", str(src), "-o", str(tmp),
+    subprocess.run(["gcc", "-O3", "-std=c11", "-fPIC", "-shared", "-ffp-contract=off", str(src), "-o", str(tmp),
                     "-lpthread"], check=True)
     os.replace(tmp, LIB_PATH)
     return LIB_PATH
