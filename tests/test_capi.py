@@ -234,3 +234,55 @@ def test_header_is_plain_c(tmp_path):
     res = subprocess.run([cc, "-std=c99", "-Wall", "-Werror", "-pedantic", "-fsyntax-only",
                           f"-I{ROOT / 'include'}", str(src)], capture_output=True, text=True)
     assert res.returncode == 0, res.stderr
+
+
+def test_c_program_links_and_runs(lib_built, tmp_path):
+    """A C program linked against libgrgx.so alone (no Python) loads a reference-written .grg,
+    reads its sizes, writes it back, reloads the copy, subsets it and reports a bad path with
+    a status and a message -- the host side of the boundary a C or C++ caller drives."""
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    lib = ROOT / "grgl_gb300" / "libgrgx.so"
+    src = tmp_path / "host_abi.c"
+    src.write_text(r'''
+#include <stdio.h>
+#include <string.h>
+#include "grgx.h"
+#define CHECK(x) do { if ((x) != GRGX_OK) { fprintf(stderr, "%s: %s\n", #x, grgx_last_error()); return 1; } } while (0)
+int main(int argc, char** argv) {
+    grgx_graph *g = NULL, *h = NULL, *s = NULL;
+    grgx_graph_info a, b, c;
+    CHECK(grgx_graph_load(argv[1], &g));
+    CHECK(grgx_graph_info_get(g, &a));
+    CHECK(grgx_graph_save(g, argv[2]));
+    CHECK(grgx_graph_load(argv[2], &h));
+    CHECK(grgx_graph_info_get(h, &b));
+    if (a.num_nodes != b.num_nodes || a.num_edges != b.num_edges || a.num_samples != b.num_samples ||
+        a.num_mutations != b.num_mutations || a.ploidy != b.ploidy) return 2;
+    const uint32_t muts[3] = {0, 1, 2};
+    CHECK(grgx_graph_subset(g, muts, 3, &s));
+    CHECK(grgx_graph_info_get(s, &c));
+    if (c.num_mutations != 3 || c.num_samples != a.num_samples) return 3;
+    grgx_graph* bad = NULL;
+    if (grgx_graph_load(argv[3], &bad) == GRGX_OK || strlen(grgx_last_error()) == 0) return 4;
+    printf("%llu %llu %llu %llu\n", (unsigned long long)a.num_nodes, (unsigned long long)a.num_edges,
+           (unsigned long long)a.num_samples, (unsigned long long)a.num_mutations);
+    grgx_graph_destroy(s);
+    grgx_graph_destroy(h);
+    grgx_graph_destroy(g);
+    return 0;
+}
+''')
+    exe = tmp_path / "host_abi"
+    res = subprocess.run([cc, "-std=c99", "-Wall", "-Werror", f"-I{ROOT / 'include'}", str(src), "-o", str(exe),
+                          str(lib), f"-Wl,-rpath,{lib.parent}"], capture_output=True, text=True)
+    assert res.returncode == 0, res.stderr
+    run = subprocess.run([str(exe), str(GOLDEN / "t200.grg"), str(tmp_path / "copy.grg"),
+                          str(tmp_path / "missing.grg")], capture_output=True, text=True, timeout=120)
+    assert run.returncode == 0, (run.returncode, run.stderr)
+    og = oracle.read_grg(GOLDEN / "t200.grg")
+    assert run.stdout.split() == [str(og.num_nodes), str(og.num_edges), str(og.num_samples), str(og.num_mutations)]
