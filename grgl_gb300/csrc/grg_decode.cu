@@ -88,7 +88,8 @@ __global__ void bucket_decode_kernel(const unsigned char* __restrict__ bytes, un
 
 unsigned blocks_for(unsigned long long items) {
     unsigned long long b = (items + 255) / 256;
-    if (b > 152ull * 32) b = 152ull * 32;
+    const unsigned long long cap = static_cast<unsigned long long>(sm_count()) * 32;
+    if (b > cap) b = cap;
     return static_cast<unsigned>(b < 1 ? 1 : b);
 }
 

@@ -125,6 +125,21 @@ std::unique_ptr<HostPlan> build_plan(const HostGraph& g);
 // (plan_device.cu), which computes heights, the renumbering, the UP adjacency and the parent
 // counts on the GPU and lays out rows and chunks here.
 void chunk_level(PullCSR& P, const std::vector<int64_t>& off, int64_t rb, int64_t re);
+// While alive, plans built on this thread size their chunks for a device with `sms` SMs.
+class PlanDeviceScope {
+  public:
+    explicit PlanDeviceScope(int sms);
+    ~PlanDeviceScope();
+    PlanDeviceScope(const PlanDeviceScope&) = delete;
+    PlanDeviceScope& operator=(const PlanDeviceScope&) = delete;
+
+  private:
+    int saved_;
+};
+// Chunks per level the chunker aims for (from the SM count in scope).
+int64_t chunk_target();
+// SM count of the current device (looked up once per device, matmul.cu).
+int sm_count();
 void finish_csr(PullCSR& P, const std::vector<int64_t>& off);
 void single_level_csr(PullCSR& P, const std::vector<std::pair<uint32_t, uint32_t>>& pairs);
 // level_begin from the node count of each height

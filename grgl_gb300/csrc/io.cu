@@ -215,7 +215,8 @@ void store_cols_t(const void* vals, long long stride, long long K, long long C, 
 
 unsigned grid_for(long long total) {
     long long b = (total + 255) / 256;
-    if (b > 152 * 32) b = 152 * 32;
+    const long long cap = static_cast<long long>(sm_count()) * 32;
+    if (b > cap) b = cap;
     return (unsigned)(b < 1 ? 1 : b);
 }
 

@@ -192,7 +192,8 @@ __global__ void init_xtx_df_kernel(const uint32_t* __restrict__ xtx, long long K
 
 unsigned grid_for(long long total) {
     long long b = (total + 255) / 256;
-    if (b > 152 * 32) b = 152 * 32;
+    const long long cap = static_cast<long long>(sm_count()) * 32;
+    if (b > cap) b = cap;
     return (unsigned)(b < 1 ? 1 : b);
 }
 

@@ -8,6 +8,9 @@
 
 namespace grgx {
 
+// SM count of the current device (looked up once per device, matmul.cu).
+int sm_count();
+
 // Storage/accumulation kinds (see ops.cuh).
 enum class Kind { U32, U64, F64, F32C, F32, XOR, F64S };
 

@@ -48,17 +48,26 @@ void parallel_for(uint64_t n, const std::function<void(uint64_t, uint64_t, int)>
 
 }  // namespace
 
-// Chunk target: enough chunks per level to give every SM several waves of warps, never
-// fewer than 64 edges per chunk.
-constexpr int64_t kTargetChunks = 152 * 16 * 8;
+// Chunk target: enough chunks per level to give every SM several waves of warps (16 warps per
+// SM, 8 chunks each), never fewer than 64 edges per chunk.  The SM count is that of the device
+// the plan is built for (PlanDeviceScope); a plan built with no device in view (host-side
+// inspection) assumes a GB300's 152 SMs.
 constexpr int64_t kMinChunk = 64;
 constexpr int64_t kMaxChunk = 1 << 22;
+constexpr int kHostOnlySms = 152;
+thread_local int t_plan_sms = 0;
+
+PlanDeviceScope::PlanDeviceScope(int sms) : saved_(t_plan_sms) { t_plan_sms = sms; }
+PlanDeviceScope::~PlanDeviceScope() { t_plan_sms = saved_; }
+
+int64_t chunk_target() { return static_cast<int64_t>(t_plan_sms > 0 ? t_plan_sms : kHostOnlySms) * 16 * 8; }
 
 void chunk_level(PullCSR& P, const std::vector<int64_t>& off, int64_t rb, int64_t re) {
     P.level_chunk_begin.push_back(static_cast<int32_t>(P.chunks.size()));
     const int64_t levelEdges = off[re] - off[rb];
     P.max_level_edges = std::max(P.max_level_edges, levelEdges);
-    int64_t C = (levelEdges + kTargetChunks - 1) / kTargetChunks;
+    const int64_t target = chunk_target();
+    int64_t C = (levelEdges + target - 1) / target;
     C = ((C + 31) / 32) * 32;
     C = std::max(kMinChunk, std::min(kMaxChunk, C));
     int64_t r = rb;

@@ -60,7 +60,8 @@ struct DevBufs {
 
 unsigned blocks_for(unsigned long long items, unsigned perBlock) {
     unsigned long long b = (items + perBlock - 1) / perBlock;
-    if (b > 152ull * 64) b = 152ull * 64;
+    const unsigned long long cap = static_cast<unsigned long long>(sm_count()) * 64;
+    if (b > cap) b = cap;
     return static_cast<unsigned>(b < 1 ? 1 : b);
 }
 

@@ -88,7 +88,7 @@ uint32_t* build_down_adj_device(const uint32_t* upAdj, const int* upRows, const 
         temps.push_back(v0);
         PLAN_CUDA(cudaMalloc(&v1, E * sizeof(uint32_t)));
         temps.push_back(v1);
-        expand_parents_kernel<<<152 * 8, 256>>>(upAdj, upRows, upChunks, upChunkCount, dRowOf, k0, v0);
+        expand_parents_kernel<<<sm_count() * 8, 256>>>(upAdj, upRows, upChunks, upChunkCount, dRowOf, k0, v0);
         PLAN_CUDA(cudaGetLastError());
         const long long R = static_cast<long long>(downOff.size()) - 1;
         int bits = 1;
@@ -101,7 +101,7 @@ uint32_t* build_down_adj_device(const uint32_t* upAdj, const int* upRows, const 
         temps.push_back(temp);
         PLAN_CUDA(cub::DeviceRadixSort::SortPairs(temp, tempBytes, keys, vals, E, 0, bits));
         result = vals.Current();
-        set_heads_kernel<<<152 * 8, 256>>>(result, dOff, R);
+        set_heads_kernel<<<sm_count() * 8, 256>>>(result, dOff, R);
         PLAN_CUDA(cudaGetLastError());
         PLAN_CUDA(cudaDeviceSynchronize());
     } catch (...) {

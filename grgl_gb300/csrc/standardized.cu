@@ -98,7 +98,8 @@ __global__ void down_finish_kernel(T* __restrict__ Y, const double* __restrict__
 
 unsigned grid_for(long long n) {
     long long b = (n + 255) / 256;
-    if (b > 152 * 32) b = 152 * 32;
+    const long long cap = static_cast<long long>(sm_count()) * 32;
+    if (b > cap) b = cap;
     return (unsigned)(b < 1 ? 1 : b);
 }
 

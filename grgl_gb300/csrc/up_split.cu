@@ -45,7 +45,8 @@ std::atomic<long long> g_block{32768};
 
 unsigned blocks_for(unsigned long long items, unsigned perBlock) {
     unsigned long long b = (items + perBlock - 1) / perBlock;
-    if (b > 152ull * 64) b = 152ull * 64;
+    const unsigned long long cap = static_cast<unsigned long long>(sm_count()) * 64;
+    if (b > cap) b = cap;
     return static_cast<unsigned>(b < 1 ? 1 : b);
 }
 
@@ -186,6 +187,7 @@ namespace {
 // Builds d.up0b / d.up_int / d.fin from the resident UP CSR (rows = nodes level_begin[1] .. n-1
 // in order, children ascending).
 void build_up_split(DevicePlan& d) {
+    const PlanDeviceScope planSms(sm_count());
     const long long block = split_block_size();
     const long long src0 = static_cast<long long>(d.level_begin[1]);
     const long long n = static_cast<long long>(d.level_begin[d.num_levels]);

@@ -3,12 +3,19 @@
 # sources where they lie under the reference checkout, into oracle/_ref/:
 #   oracle/_ref/_grgl*.so     the reference Python module (pygrgl's `_grgl`), -O3 -DNDEBUG
 #   oracle/_ref/ref_construct VCF/IGD -> .grg with the reference constructor
-# Needs the reference checkout (GRGL_REF, default /root/reference) and pip pybind11; it is
-# only run where both exist.  Nothing here is copied into the repository.
+#   oracle/_ref/src           a link to the checkout (its test inputs and expected outputs)
+#   oracle/_ref/pygrgl        a link to the checkout's Python package (which imports _grgl)
+# Needs the reference checkout (GRGL_REF, default /root/reference) and pip pybind11.  Where the
+# checkout is absent it does nothing and exits 0.  Nothing here is copied into the repository.
 set -euo pipefail
 REF=${GRGL_REF:-/root/reference}
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT=$HERE/_ref
+if [ ! -f "$REF/include/grgl/grg.h" ]; then
+  echo "reference checkout not found ($REF): oracle/_ref not built"
+  exit 0
+fi
+python3 -c 'import pybind11' 2>/dev/null || { echo "pybind11 missing: oracle/_ref not built"; exit 0; }
 OBJ=$OUT/obj
 mkdir -p "$OBJ"
 PYINC=$(python3 -c 'import sysconfig; print(sysconfig.get_paths()["include"])')
@@ -36,4 +43,6 @@ for s in $SRCS; do CORE="$CORE $OBJ/$s.o"; done
 CORE="$CORE $OBJ/snp_hwe.o $OBJ/vbyte.o $OBJ/varintdecode.o $OBJ/tsk_stubs.o"
 g++ -shared -o "$OUT/_grgl$EXT" "$OBJ/_grgl.o" $CORE -lz -lpthread
 g++ -o "$OUT/ref_construct" "$OBJ/ref_construct.o" $CORE -lz -lpthread
+ln -sfn "$REF" "$OUT/src"
+ln -sfn "$REF/pygrgl" "$OUT/pygrgl"
 echo "built $OUT/_grgl$EXT and $OUT/ref_construct"

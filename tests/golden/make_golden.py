@@ -1,7 +1,7 @@
 """Regenerate the golden fixtures from the reference GRGL itself.
 
-Run where the reference checkout exists (GRGL_REF, default /root/reference) after
-``oracle/build_ref.sh`` has compiled it into oracle/_ref:
+Run after ``oracle/build_ref.sh`` has compiled the reference into oracle/_ref (it also links
+the reference checkout there as oracle/_ref/src and its Python package as oracle/_ref/pygrgl):
 
     python tests/golden/make_golden.py
 
@@ -20,7 +20,6 @@ from __future__ import annotations
 
 import gzip
 import json
-import os
 import subprocess
 import sys
 from pathlib import Path
@@ -29,8 +28,8 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 ROOT = HERE.parent.parent
-REF = Path(os.environ.get("GRGL_REF", "/root/reference"))
-sys.path[:0] = [str(ROOT / "oracle" / "_ref"), str(REF), str(ROOT)]
+REF = ROOT / "oracle" / "_ref" / "src"
+sys.path[:0] = [str(ROOT / "oracle" / "_ref"), str(ROOT)]
 
 import pygrgl  # noqa: E402  (the reference module built by oracle/build_ref.sh)
 

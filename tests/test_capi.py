@@ -192,18 +192,16 @@ def test_save_round_trip(gx, tmp_path):
 
 
 def test_saved_file_reads_in_the_reference(gx, tmp_path):
-    import os
     import sys
 
     ref = ROOT / "oracle" / "_ref"
-    src = os.environ.get("GRGL_REF", "/root/reference")
-    if not (ref.exists() and os.path.isdir(src)):
-        pytest.skip("reference build not present")
-    sys.path[:0] = [str(ref), src]
+    if not (ref / "pygrgl").is_dir():
+        pytest.skip("reference build not present (oracle/build_ref.sh)")
+    sys.path[:0] = [str(ref)]
     try:
         pygrgl = pytest.importorskip("pygrgl")
     finally:
-        del sys.path[:2]
+        del sys.path[:1]
     g = gx.window_tree_grg(500, 3000, seed=5)
     path = str(tmp_path / "wt.grg")
     g.save(path)
