@@ -67,6 +67,7 @@ SIGNATURES = {
     "grgx_server_submit": (_int, [_vp, _u32, ctypes.POINTER(Request), ctypes.POINTER(_u64)]),
     "grgx_server_wait": (_int, [_vp, _u64, ctypes.c_double, ctypes.POINTER(RequestStats)]),
     "grgx_server_destroy": (None, [_vp]),
+    "grgx_pool_usage": (_int, [_int, ctypes.POINTER(_u64), ctypes.POINTER(_u64)]),
     "grgx_measure_l2_bandwidth": (_int, [_u64, _int, ctypes.POINTER(ctypes.c_double)]),
     "grgx_host_alloc": (_int, [_u64, ctypes.POINTER(_vp)]),
     "grgx_host_free": (None, [_vp]),

@@ -456,6 +456,14 @@ def measure_l2_bandwidth(nbytes: int = 48 << 20, reps: int = 40) -> float:
     return v.value
 
 
+def pool_usage(device: int = 0) -> dict:
+    """Bytes of the library's own device memory pool on `device`: handed out to calls in flight
+    (`used`) and held from the device (`reserved`, cached between calls)."""
+    u, r = ctypes.c_uint64(), ctypes.c_uint64()
+    _lib.check(_lib.lib().grgx_pool_usage(int(device), ctypes.byref(u), ctypes.byref(r)))
+    return {"used": u.value, "reserved": r.value}
+
+
 def set_timing(enabled):
     """Per-call CUDA-event timing on this thread: True (read back per call, see last_timing),
     "deferred" (no per-call sync, see collect_timings) or False."""

@@ -17,6 +17,7 @@ void set_timing(int enabled);
 grgx_timing last_timing();
 std::vector<grgx_timing> collect_timings();
 double measure_l2_bandwidth(uint64_t bytes, int reps);
+void pool_usage(int device, uint64_t* used, uint64_t* reserved);
 void matmul_noalloc_impl(grgx_graph* g, int dtype, const void* input, uint64_t in_cols, uint64_t rows, int direction,
                          void* output, uint64_t output_size, void* stream);
 void matmul_batch_impl(grgx_graph* g, const grgx_request* reqs, uint64_t n, uint64_t maxCols, uint32_t flags,
@@ -311,6 +312,10 @@ grgx_status grgx_matmul_noalloc(grgx_graph* g, grgx_dtype dtype, const void* inp
         GRGX_CHECK(g && input && output, GRGX_ERR_API_MISUSE, "null argument");
         matmul_noalloc_impl(g, dtype, input, input_cols, input_rows, direction, output, output_size, stream);
     });
+}
+
+grgx_status grgx_pool_usage(int device, uint64_t* used, uint64_t* reserved) {
+    return guarded([&] { pool_usage(device, used, reserved); });
 }
 
 grgx_status grgx_measure_l2_bandwidth(uint64_t bytes, int reps, double* gbps) {

@@ -91,8 +91,6 @@ LevelShape level_shape(const Layout& L, const DevCSR& c, size_t level);
 // work counters and of the heavy-row tickets.
 int max_tiles(const Layout& L);
 
-int sm_count();
-
 // Launches one level of a CSR (a no-op when the level has no chunks); `work` points at
 // `tileStride` (0: L.ntiles) zeroed counters owned by this launch, and the heavy-row tickets
 // are `tileStride` apart.  `shape` null: the default shape.  Returns the kernels launched.
@@ -121,10 +119,19 @@ bool up_split_possible(const DevicePlan* dp);
 void ensure_up_split(grgx_graph* g, DevicePlan* dp);
 void set_up_split_choice(grgx_graph* g, DevicePlan* dp, const Layout& L, bool split);
 
+// Resolves (once per device, with `device` current) the address of grgx_matmul_noalloc's
+// static scratch, which loads its module and so reserves the array on the device.
+void noalloc_prepare_device(int device);
+
 // Builds (once) and returns the graph's plan on the current device.
 DevicePlan* ensure_device_plan(grgx_graph* g);
 
-// cudaMallocAsync from the device's stream-ordered pool.  The pool never makes a call wait for
+// The library's own stream-ordered memory pool on `device` (created on first use).
+cudaMemPool_t library_pool(int device);
+// Bytes of the library pool on `device` handed out to calls now, and held by the pool.
+void pool_usage(int device, uint64_t* used, uint64_t* reserved);
+
+// Stream-ordered allocation from the library's pool on the current device.  The pool never makes a call wait for
 // a call on another stream, so under memory pressure the blocks such calls have freed can still
 // be in flight: then the device is drained once and the allocation retried (not inside a stream
 // capture, where the first error stands).

@@ -11,6 +11,7 @@
 // stream-ordered memory pool and is released on the same stream.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstring>
 #include <map>
 #include <sstream>
@@ -69,25 +70,35 @@ DevCSR upload_csr(DevicePlan& d, const PullCSR& c) {
     return r;
 }
 
-void setup_pool_once(int device) {
+}  // namespace
+
+// The library's own stream-ordered pool on `device` (created once per device; the process's
+// default pool, which the host application may use too, is left as it is).  Memory freed into it
+// stays cached for the next call (release threshold: never).  Calls on different streams are not
+// chained through it: a block freed by a call still running on one stream is not handed to
+// another stream's call (which would make it wait for the first); only blocks whose free has
+// completed are.
+cudaMemPool_t library_pool(int device) {
+    constexpr int kMaxDev = 64;
     static std::mutex mu;
-    static std::vector<int> done;
+    static cudaMemPool_t pools[kMaxDev] = {};
+    GRGX_CHECK(device >= 0 && device < kMaxDev, GRGX_ERR_UNSUPPORTED, "device index out of range");
     std::lock_guard<std::mutex> lk(mu);
-    for (int d : done)
-        if (d == device) return;
-    cudaMemPool_t pool;
-    GRGX_CUDA(cudaDeviceGetDefaultMemPool(&pool, device));
+    if (pools[device] != nullptr) return pools[device];
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.handleTypes = cudaMemHandleTypeNone;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = device;
+    cudaMemPool_t pool = nullptr;
+    GRGX_CUDA(cudaMemPoolCreate(&pool, &props));
     uint64_t threshold = UINT64_MAX;
     GRGX_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &threshold));
-    // Calls on different streams must not be chained through the pool: a block freed by a call
-    // still running on one stream is not handed to another stream's call (which would make it
-    // wait for the first), only blocks whose free has completed are.
     int noChain = 0;
     GRGX_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolReuseAllowInternalDependencies, &noChain));
-    done.push_back(device);
+    pools[device] = pool;
+    return pool;
 }
-
-}  // namespace
 
 long long next_pow2(long long x) {
     long long p = 1;
@@ -152,13 +163,19 @@ thread_local std::vector<PendingTiming> t_pending;
 
 }  // namespace
 
+// SM count of the current device (looked up once per device).
 int sm_count() {
-    static int sms = 0;
+    constexpr int kMaxDev = 64;
+    static std::atomic<int> cache[kMaxDev];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= kMaxDev) dev = 0;
+    int sms = cache[dev].load(std::memory_order_relaxed);
     if (sms == 0) {
-        int dev = 0, v = 0;
-        cudaGetDevice(&dev);
+        int v = 0;
         cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
         sms = v > 0 ? v : 1;
+        cache[dev].store(sms, std::memory_order_relaxed);
     }
     return sms;
 }
@@ -281,23 +298,36 @@ uint32_t* device_plan_build(const HostGraph& hg, std::unique_ptr<HostPlan>& out)
 }  // namespace
 
 cudaError_t pool_malloc(void** p, size_t bytes, cudaStream_t s) {
-    cudaError_t e = cudaMallocAsync(p, bytes, s);
+    int device = 0;
+    cudaError_t e = cudaGetDevice(&device);
+    if (e != cudaSuccess) return e;
+    const cudaMemPool_t pool = library_pool(device);
+    e = cudaMallocFromPoolAsync(p, bytes, pool, s);
     if (e != cudaErrorMemoryAllocation) return e;
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     if (cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return e;
     cudaGetLastError();
     const cudaError_t se = cudaDeviceSynchronize();
     if (se != cudaSuccess) return se;
-    return cudaMallocAsync(p, bytes, s);
+    return cudaMallocFromPoolAsync(p, bytes, pool, s);
 }
 
 void trim_pool() {
     int device = 0;
-    cudaMemPool_t pool;
-    if (cudaGetDevice(&device) != cudaSuccess || cudaDeviceGetDefaultMemPool(&pool, device) != cudaSuccess) return;
+    if (cudaGetDevice(&device) != cudaSuccess) return;
+    const cudaMemPool_t pool = library_pool(device);
     cudaDeviceSynchronize();
     cudaMemPoolTrimTo(pool, 0);
     cudaGetLastError();
+}
+
+void pool_usage(int device, uint64_t* used, uint64_t* reserved) {
+    const cudaMemPool_t pool = library_pool(device);
+    uint64_t u = 0, r = 0;  // the pool attributes are 64-bit values
+    GRGX_CUDA(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &u));
+    GRGX_CUDA(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &r));
+    if (used) *used = static_cast<uint64_t>(u);
+    if (reserved) *reserved = static_cast<uint64_t>(r);
 }
 
 namespace {
@@ -310,7 +340,9 @@ DevicePlan* ensure_device_plan_once(grgx_graph* g) {
                    "graph is resident on device " + std::to_string(g->dev->device));
         return g->dev.get();
     }
-    setup_pool_once(device);
+    library_pool(device);
+    noalloc_prepare_device(device);
+    const PlanDeviceScope planSms(sm_count());
     uint32_t* upAdjDev = nullptr;
     if (!g->plan && !g->host_plan && g->host->num_nodes > 0) upAdjDev = device_plan_build(*g->host, g->plan);
     if (!g->plan) g->plan = build_plan(g->host_edges());

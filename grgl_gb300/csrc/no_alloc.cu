@@ -6,14 +6,25 @@
 // or code that must not grow its footprint while it serves requests.  This entry point runs the
 // same kernels as grgx_matmul, but every byte of scratch it needs -- the node values, the
 // per-mutation input rows of a DOWN product, the heavy-row partial sums and the work counters --
-// is carved from one file-scope __device__ array of GRGX_NOALLOC_SCRATCH_BYTES bytes.  That array
-// exists on every GPU that loads the library, for the life of the process.
+// is carved from one file-scope __device__ array of GRGX_NOALLOC_SCRATCH_BYTES bytes.
+//
+// When the array takes device memory: CUDA loads a library's device code per device on first
+// use (lazy module loading, the default of this CUDA runtime), and the array is reserved when
+// the module holding it loads on that device.  That happens when a graph first becomes resident
+// on the device (grgx_graph_upload, or the first call that uploads it): the upload resolves the
+// array's address there, with the device current.  From then on the device holds the array
+// until the process exits.  With CUDA_MODULE_LOADING=EAGER in the environment it is reserved
+// on every device when the CUDA context is created instead.  A caller that claims its device
+// budget should upload its graphs first.
 //
 // Rules of use:
 //   * The graph must already be resident on the current device (grgx_graph_upload).
 //   * Input and output are device pointers; the output is overwritten, not added to.
-//   * The first call on a device looks up the array's device address (cudaGetSymbolAddress, with
-//     that device current); make that first call before any stream capture.
+//   * The array's device address is looked up once per device (cudaGetSymbolAddress, with that
+//     device current) by the graph upload; a call on a device where that has not happened yet
+//     looks it up itself, so make the first call before any stream capture.
+//   * A device reset (cudaDeviceReset) between calls is not supported: the address looked up
+//     before it would be stale.
 //   * Every call shares the one array and leaves its contents behind; the call clears what must
 //     start at zero itself.  Calls whose work overlaps on the GPU (different streams, or
 //     different host threads) race on the array: serialise them on one stream.
@@ -65,6 +76,10 @@ struct Carve {
 
 }  // namespace
 
+// Called with `device` current when a graph becomes resident there: loads this file's module
+// on the device, which reserves the static scratch, and caches its address.
+void noalloc_prepare_device(int device) { scratch_address(device); }
+
 void matmul_noalloc_impl(grgx_graph* g, int dtype, const void* input, uint64_t in_cols, uint64_t rows, int direction,
                          void* output, uint64_t output_size, void* stream_ptr) {
     const HostGraph& hg = *g->host;
@@ -89,7 +104,11 @@ void matmul_noalloc_impl(grgx_graph* g, int dtype, const void* input, uint64_t i
     GRGX_CHECK(rows <= 2000000ull, GRGX_ERR_UNSUPPORTED, "too many input rows for one call; split the rows");
     int device = 0;
     GRGX_CUDA(cudaGetDevice(&device));
-    const DevicePlan* dp = g->dev.get();
+    const DevicePlan* dp = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g->mu);  // the upload writes g->dev under this lock
+        dp = g->dev.get();
+    }
     GRGX_CHECK(dp != nullptr && dp->device == device, GRGX_ERR_UNSUPPORTED,
                "grgx_matmul_noalloc needs the graph resident on the current device: call grgx_graph_upload first");
 

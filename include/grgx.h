@@ -238,8 +238,9 @@ grgx_status grgx_server_wait(grgx_server* s, uint64_t ticket, double timeout_s, 
 /* Stops the workers after the batches in flight; queued requests fail with GRGX_ERR_TIMEOUT. */
 void grgx_server_destroy(grgx_server* s);
 
-/* Size of the static device scratch behind grgx_matmul_noalloc (64 MiB on every GPU that loads
- * the library, held until the process exits). */
+/* Size of the static device scratch behind grgx_matmul_noalloc (64 MiB).  A device holds it
+ * from the first graph upload on that device (CUDA loads device code lazily, per device; with
+ * CUDA_MODULE_LOADING=EAGER from context creation) until the process exits. */
 #define GRGX_NOALLOC_SCRATCH_BYTES (64ull << 20)
 
 /* No counterpart in the reference.  The plain product (no init, miss, emit_all_nodes or
@@ -249,12 +250,23 @@ void grgx_server_destroy(grgx_server* s);
  * GRGX_NOALLOC_SCRATCH_BYTES, and products that need more are rejected with
  * GRGX_ERR_UNSUPPORTED before any launch.  input/output are device pointers; the output is
  * overwritten; the call is asynchronous on `stream`.  The graph must already be resident
- * (grgx_graph_upload).  The first call on each device looks up the array's address; make it
- * before any stream capture.  All calls share the array: calls that overlap on the GPU race,
- * so serialise them on one stream.  bool is not supported. */
+ * (grgx_graph_upload); the upload also reserves the static array on the device and looks up
+ * its address, so upload graphs before claiming the rest of a device budget.  (A call on a
+ * device where no upload happened looks the address up itself; make such a first call before
+ * any stream capture.)  All calls share the array: calls that overlap on the GPU race, so
+ * serialise them on one stream.  A device reset between calls is not supported.  float64
+ * accumulates on the FP64 pipe (grgx_matmul's float64 default is the scaled float-pair path,
+ * GRGX_FLAG_F64_NATIVE selects the same FP64 accumulation there).  bool is not supported. */
 grgx_status grgx_matmul_noalloc(grgx_graph* g, grgx_dtype dtype, const void* input, uint64_t input_cols,
                                 uint64_t input_rows, grgx_direction direction, void* output, uint64_t output_size,
                                 void* stream);
+
+/* No counterpart in the reference.  Device memory of the library's own stream-ordered pool on
+ * `device` (the per-call scratch of grgx_matmul and the batch, server and operator entries):
+ * `used` = bytes handed out to calls in flight, `reserved` = bytes the pool holds from the
+ * device (kept cached between calls).  Either pointer may be NULL.  The process's default pool
+ * is not used or changed by the library. */
+grgx_status grgx_pool_usage(int device, uint64_t* used, uint64_t* reserved);
 
 /* Diagnostic, no counterpart in the reference: measured L2 -> SM read bandwidth (GB/s) of the
  * current device over an L2-resident buffer of `bytes` (>= 1 MiB) read `reps` times -- the
