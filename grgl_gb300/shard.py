@@ -23,8 +23,10 @@ from .api import DOWN, GRG, UP, TraversalDirection, matmul
 MatmulFn = Callable[..., np.ndarray]
 
 
-def mutation_ranges(grg: GRG, nshards: int) -> List[range]:
-    """Contiguous mutation id ranges with about the same number of edges below each."""
+def mutation_ranges(grg: GRG, nshards: int, align: int = 1) -> List[range]:
+    """Contiguous mutation id ranges with about the same number of edges below each.  With
+    `align` > 1 every boundary is rounded to a multiple of it (e.g. the window of a window-tree
+    graph, so that no two ranges share a node with children)."""
     a = grg.export_arrays()
     off, mut = a["down_off"], a["mut_node"]
     deg = np.diff(off.astype(np.int64))
@@ -34,7 +36,10 @@ def mutation_ranges(grg: GRG, nshards: int) -> List[range]:
     cum = np.concatenate([[0.0], np.cumsum(w)])
     bounds = [0]
     for s in range(1, nshards):
-        bounds.append(int(np.searchsorted(cum, cum[-1] * s / nshards)))
+        b = int(np.searchsorted(cum, cum[-1] * s / nshards))
+        if align > 1:
+            b = min(len(mut), (b + align // 2) // align * align)
+        bounds.append(b)
     bounds.append(len(mut))
     bounds = sorted(set(bounds))
     return [range(bounds[i], bounds[i + 1]) for i in range(len(bounds) - 1)]
@@ -80,31 +85,64 @@ class ShardedGRG:
         return out.cpu().numpy() if host else out
 
 
-def distributed_matmul(shards: Sequence[GRG], ranges: Sequence[range], owned: Sequence[int], V: np.ndarray,
+def distributed_matmul(shards: Sequence[GRG], ranges: Sequence[range], owned: Sequence[int], V,
                        direction, num_samples: int, num_mutations: int, matmul_fn: MatmulFn = matmul):
     """Product over shards spread across torch.distributed ranks.
 
     Every rank passes the full input `V`, the shard list and `owned`, the indices of the shards it
     computes.  UP: each rank fills its shards' column blocks, the blocks are summed across ranks
-    (disjoint, so the sum is an all-gather); DOWN: per-rank partial sums are all-reduced.
+    (disjoint, so the sum is an all-gather); DOWN: per-rank partial sums are all-reduced.  `V`
+    may be a numpy array (host tensors: the gloo backend) or a CUDA tensor (the partial outputs
+    stay on the device and are reduced there: the nccl backend); the result has V's kind.  bool
+    inputs combine in GF(2): partials are added as bytes and reduced mod 2.
     """
     import torch
     import torch.distributed as dist
 
     direction = TraversalDirection(int(direction))
-    K = V.shape[0]
-    if direction == UP:
-        out = np.zeros((K, num_mutations), dtype=V.dtype)
-        for i in owned:
-            out[:, ranges[i].start:ranges[i].stop] = np.asarray(matmul_fn(shards[i], V, UP))
-    else:
-        out = np.zeros((K, num_samples), dtype=V.dtype)
-        for i in owned:
-            part = np.ascontiguousarray(V[:, ranges[i].start:ranges[i].stop])
-            out += np.asarray(matmul_fn(shards[i], part, DOWN))
-    t = torch.from_numpy(out)
-    if t.dtype == torch.bool:
-        t = t.to(torch.uint8)
-    dist.all_reduce(t, op=dist.ReduceOp.SUM)
-    res = t.numpy()
-    return res.astype(V.dtype) if res.dtype != V.dtype else res
+    is_tensor = isinstance(V, torch.Tensor)
+    X = V if is_tensor else torch.from_numpy(np.ascontiguousarray(V))
+    gf2 = X.dtype == torch.bool
+    acc_dtype = torch.uint8 if gf2 else X.dtype
+    K = X.shape[0]
+    out = torch.zeros((K, num_mutations if direction == UP else num_samples), dtype=acc_dtype, device=X.device)
+
+    def run(i, cols):
+        src = V[:, cols.start:cols.stop] if direction == DOWN else V
+        if not is_tensor:
+            src = np.ascontiguousarray(src)
+        elif direction == DOWN:
+            src = src.contiguous()
+        res = matmul_fn(shards[i], src, direction)
+        return torch.as_tensor(np.asarray(res) if not isinstance(res, torch.Tensor) else res,
+                               device=X.device).to(acc_dtype)
+
+    for i in owned:
+        r = ranges[i]
+        if direction == UP:
+            out[:, r.start:r.stop] = run(i, r)
+        else:
+            out += run(i, r)
+    dist.all_reduce(out, op=dist.ReduceOp.SUM)
+    if gf2:
+        out = (out & 1).to(torch.bool)
+    return out if is_tensor else out.numpy()
+
+
+def combine_rank_output(out, direction, ranges: Sequence[range]):
+    """The whole product from this rank's product over its own range (rank r of the process group
+    owns ranges[r]): DOWN partial sums are all-reduced in place; UP column blocks, which differ in
+    width, are all-gathered padded to the widest and concatenated in range order.  `out` is a
+    torch tensor (CUDA under nccl, host under gloo)."""
+    import torch
+    import torch.distributed as dist
+
+    if int(direction) == int(DOWN):
+        dist.all_reduce(out, op=dist.ReduceOp.SUM)
+        return out
+    widest = max(len(r) for r in ranges)
+    block = torch.zeros((out.shape[0], widest), dtype=out.dtype, device=out.device)
+    block[:, :out.shape[1]] = out
+    parts = [torch.empty_like(block) for _ in range(len(ranges))]
+    dist.all_gather(parts, block)
+    return torch.cat([p[:, :len(r)] for p, r in zip(parts, ranges)], dim=1)

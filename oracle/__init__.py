@@ -17,6 +17,7 @@ import ctypes
 import os
 import subprocess
 import threading
+import weakref
 from dataclasses import dataclass
 from pathlib import Path
 from typing import Optional
@@ -36,22 +37,38 @@ _DTYPES = {
 }
 
 
+SOURCES = ("grg_oracle.c", "window_tree.c")
+
+
 def build(force: bool = False) -> Path:
-    """Compile liboracle.so from grg_oracle.c (gcc, no FMA contraction)."""
-    src = HERE / "grg_oracle.c"
-    if not force and LIB_PATH.exists() and LIB_PATH.stat().st_mtime >= src.stat().st_mtime:
+    """Compile liboracle.so from grg_oracle.c and window_tree.c (gcc, no FMA contraction)."""
+    srcs = [HERE / f for f in SOURCES]
+    if not force and LIB_PATH.exists() and all(LIB_PATH.stat().st_mtime >= s.stat().st_mtime for s in srcs):
         return LIB_PATH
-    tmp = LIB_PATH.with_suffix(".so.tmp")
-    subprocess.run(["gcc", "-O3", "-std=c11", "-fPIC", "-shared", "-ffp-contract=off", str(src), "-o", str(tmp),
-                    "-lpthread"], check=True)
+    tmp = LIB_PATH.with_suffix(f".so.tmp{os.getpid()}")
+    subprocess.run(["gcc", "-O3", "-std=c11", "-fPIC", "-shared", "-ffp-contract=off", *map(str, srcs), "-o",
+                    str(tmp), "-lpthread"], check=True)
     os.replace(tmp, LIB_PATH)
     return LIB_PATH
+
+
+def host_threads() -> int:
+    """Host cores this process may run on."""
+    try:
+        return max(1, len(os.sched_getaffinity(0)))
+    except AttributeError:
+        return max(1, os.cpu_count() or 1)
 
 
 class _Graph(ctypes.Structure):
     _fields_ = [("num_nodes", ctypes.c_uint64), ("num_samples", ctypes.c_uint64), ("ploidy", ctypes.c_uint64),
                 ("num_mutations", ctypes.c_uint64), ("down_off", ctypes.c_void_p), ("down_adj", ctypes.c_void_p),
                 ("mut_node", ctypes.c_void_p), ("miss_node", ctypes.c_void_p), ("coals", ctypes.c_void_p)]
+
+
+class _WTGraph(ctypes.Structure):
+    _fields_ = [("num_nodes", ctypes.c_uint64), ("num_edges", ctypes.c_uint64), ("num_mutations", ctypes.c_uint64),
+                ("down_off", ctypes.c_void_p), ("down_adj", ctypes.c_void_p), ("mut_node", ctypes.c_void_p)]
 
 
 _lib = None
@@ -69,13 +86,21 @@ def _load():
             lib.oracle_matmul.argtypes = [ctypes.POINTER(_Graph), ctypes.c_int, ctypes.c_void_p, ctypes.c_uint64,
                                           ctypes.c_uint64, ctypes.c_int, ctypes.c_void_p, ctypes.c_uint64,
                                           ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
-            lib.oracle_shards_create.restype = ctypes.c_void_p
-            lib.oracle_shards_create.argtypes = [ctypes.POINTER(_Graph), ctypes.c_int]
+            lib.oracle_shards_create_mt.restype = ctypes.c_void_p
+            lib.oracle_shards_create_mt.argtypes = [ctypes.POINTER(_Graph), ctypes.c_int, ctypes.c_int,
+                                                    ctypes.c_uint64]
             lib.oracle_shards_destroy.argtypes = [ctypes.c_void_p]
-            lib.oracle_matmul_sharded.restype = ctypes.c_int
-            lib.oracle_matmul_sharded.argtypes = [ctypes.POINTER(_Graph), ctypes.c_void_p, ctypes.c_int,
-                                                  ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int,
-                                                  ctypes.c_void_p, ctypes.c_uint64]
+            lib.oracle_shard_edges.restype = ctypes.c_uint64
+            lib.oracle_shard_edges.argtypes = [ctypes.c_void_p, ctypes.c_int]
+            lib.oracle_matmul_shard_range.restype = ctypes.c_int
+            lib.oracle_matmul_shard_range.argtypes = [ctypes.POINTER(_Graph), ctypes.c_void_p, ctypes.c_int,
+                                                      ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_uint64,
+                                                      ctypes.c_uint64, ctypes.c_int, ctypes.c_void_p,
+                                                      ctypes.c_uint64, ctypes.POINTER(ctypes.c_double)]
+            lib.oracle_window_tree.restype = ctypes.c_int
+            lib.oracle_window_tree.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint32,
+                                               ctypes.c_int, ctypes.POINTER(_WTGraph)]
+            lib.oracle_window_tree_free.argtypes = [ctypes.POINTER(_WTGraph)]
             _lib = lib
     return _lib
 
@@ -209,29 +234,88 @@ def matmul(g: OracleGraph, input, direction: int, emit_all_nodes: bool = False, 
 
 
 class Shards:
-    """The reference's range-split multi-core pattern (test/endtoend/test_matmul.py:264-325)."""
+    """The reference's range-split multi-core pattern (test/endtoend/test_matmul.py:264-325): the
+    mutations cut into `nshards` contiguous ranges, each range's sub-graph (the nodes below its
+    mutations, what saveGRGSubset keeps) multiplied on its own thread, DOWN partial outputs
+    summed in shard order, UP outputs disjoint.  Range starts are rounded to multiples of
+    `align` mutations (the window of a window-tree graph: then no two shards share a node with
+    children).  `build_threads` threads build the shards."""
 
-    def __init__(self, g: OracleGraph, nshards: int):
+    def __init__(self, g: OracleGraph, nshards: int, build_threads: int = 0, align: int = 1):
         self.g = g
         self._gs = g._struct()
-        self.ptr = _load().oracle_shards_create(ctypes.byref(self._gs), int(nshards))
+        self.ptr = _load().oracle_shards_create_mt(ctypes.byref(self._gs), int(nshards),
+                                                   int(build_threads or host_threads()), int(align))
         _check(bool(self.ptr), "sharding needs a topologically ordered graph")
         self.nshards = nshards
+        self.last_reduce_s = 0.0
 
-    def matmul(self, input: np.ndarray, direction: int) -> np.ndarray:
+    def edges(self, first: int = 0, count: Optional[int] = None) -> int:
+        """Edges the shards [first, first + count) traverse."""
+        count = self.nshards - first if count is None else count
+        lib = _load()
+        return sum(int(lib.oracle_shard_edges(self.ptr, i)) for i in range(first, first + count))
+
+    def matmul(self, input: np.ndarray, direction: int, first: int = 0, count: Optional[int] = None) -> np.ndarray:
+        """The product over shards [first, first + count) (all by default), one thread per shard;
+        the DOWN partial-sum time is left in `last_reduce_s`."""
         arr = np.ascontiguousarray(input)
         rows, cols = arr.shape
+        count = self.nshards - first if count is None else count
         out_cols = self.g.num_samples if int(direction) == DOWN else self.g.num_mutations
         out = np.zeros((rows, out_cols), dtype=arr.dtype)
-        rc = _load().oracle_matmul_sharded(ctypes.byref(self._gs), self.ptr, _DTYPES[arr.dtype], arr.ctypes.data,
-                                           cols, rows, int(direction), out.ctypes.data, out_cols)
+        red = ctypes.c_double(0.0)
+        rc = _load().oracle_matmul_shard_range(ctypes.byref(self._gs), self.ptr, int(first), int(count),
+                                               _DTYPES[arr.dtype], arr.ctypes.data, cols, rows, int(direction),
+                                               out.ctypes.data, out_cols, ctypes.byref(red))
         _check(rc == 0, f"oracle failure {rc}")
+        self.last_reduce_s = red.value
         return out
 
     def __del__(self):
         if getattr(self, "ptr", None):
             _load().oracle_shards_destroy(self.ptr)
             self.ptr = None
+
+
+def _owned(ptr: int, count: int, ctype, free_fn) -> np.ndarray:
+    """A numpy view of `count` elements at `ptr` that frees the block (free_fn) when the last
+    view of it goes away."""
+    if count == 0:
+        free_fn(ptr)
+        return np.zeros(0, dtype=ctype)
+    buf = (np.ctypeslib.as_ctypes_type(ctype) * count).from_address(ptr)
+    weakref.finalize(buf, free_fn, ptr)
+    return np.frombuffer(buf, dtype=ctype)
+
+
+def window_tree(num_samples: int, num_mutations: int, seed: int = 42, window: int = 100,
+                threads: int = 0) -> OracleGraph:
+    """The seeded window-tree graph (window_tree.c), generated on `threads` host threads (all by
+    default) without the product library: the same graph the product's generator makes."""
+    lib = _load()
+    wt = _WTGraph()
+    rc = lib.oracle_window_tree(int(num_samples), int(num_mutations), int(seed), int(window),
+                                int(threads or host_threads()), ctypes.byref(wt))
+    _check(rc == 0, f"window-tree generator failed ({rc})")
+    libc_free = _libc_free()
+    off = _owned(wt.down_off, int(wt.num_nodes) + 1, np.uint64, libc_free)
+    adj = _owned(wt.down_adj, int(wt.num_edges), np.uint32, libc_free)
+    mut = _owned(wt.mut_node, int(wt.num_mutations), np.uint32, libc_free)
+    return OracleGraph(num_samples=int(num_samples), ploidy=2, down_off=off, down_adj=adj, mut_node=mut)
+
+
+_free = None
+
+
+def _libc_free():
+    global _free
+    if _free is None:
+        f = ctypes.CDLL(None).free
+        f.argtypes = [ctypes.c_void_p]
+        f.restype = None
+        _free = f
+    return _free
 
 
 # ---- independent .grg reader ------------------------------------------------------------------

@@ -27,10 +27,12 @@
  * each range's sub-graph (the nodes below its mutations) is multiplied on its own thread,
  * DOWN partial outputs are summed and UP outputs are disjoint.
  */
+#define _POSIX_C_SOURCE 199309L
 #include <pthread.h>
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 
 #define ORACLE_INVALID_NODE 0x7fffffffu
 #define ORACLE_COAL_NOT_SET 0xffffffffu
@@ -127,7 +129,7 @@ static uint32_t* children_first_order(const oracle_graph* g) {
                           T* miss, const uint8_t* active, const triple_t* trip, uint64_t ntrip,                \
                           const uint32_t* order) {                                                             \
         const uint64_t n = g->num_nodes, K = rows;                                                             \
-        T* val = (T*)calloc(n * K ? n * K : 1, sizeof(T));                                                     \
+        T* val = (T*)calloc((n * K) != 0 ? n * K : 1, sizeof(T));                                                   \
         if (!val) return -1;                                                                                   \
         switch (init_kind) {                                                                                   \
         case OR_INIT_XTX:                                                                                      \
@@ -222,7 +224,7 @@ static int matmul_bool(const oracle_graph* g, const uint8_t* in, uint64_t in_col
                        uint8_t* out, uint64_t out_cols, int emit_all, int by_indiv, uint8_t* miss,
                        const uint8_t* active, const triple_t* trip, uint64_t ntrip, const uint32_t* order) {
     const uint64_t n = g->num_nodes, K = rows;
-    uint8_t* val = (uint8_t*)calloc(n * K ? n * K : 1, 1);
+    uint8_t* val = (uint8_t*)calloc((n * K) != 0 ? n * K : 1, 1);
     if (!val) return -1;
     if (direction == OR_DOWN) {
         for (uint64_t t = 0; t < ntrip; t++) {
@@ -316,7 +318,7 @@ int oracle_matmul(const oracle_graph* g, int dtype, const void* in, uint64_t in_
     return rc;
 }
 
-/* ---- sharded multi-core form (CPU baseline only) ---------------------------------------- */
+/* ---- sharded multi-core form ------------------------------------------------------------ */
 
 typedef struct {
     const oracle_graph* g;
@@ -326,7 +328,6 @@ typedef struct {
     int direction;
     void* out; /* private DOWN partial or shared UP output */
     uint64_t out_cols;
-    const uint8_t* active;
     const triple_t* trip;
     uint64_t ntrip;
     int rc;
@@ -335,63 +336,171 @@ typedef struct {
 static void* shard_main(void* arg) {
     shard_job* j = (shard_job*)arg;
     j->rc = dispatch(j->g, j->dtype, j->in, j->in_cols, j->rows, j->direction, j->out, j->out_cols, 0, 0, NULL,
-                     OR_INIT_ZERO, NULL, j->active, j->trip, j->ntrip, NULL);
+                     OR_INIT_ZERO, NULL, NULL, j->trip, j->ntrip, NULL);
     return NULL;
 }
 
+/* One shard: the sub-graph that saveGRGSubset keeps for a mutation range (serialize.h:147-166):
+ * every sample, and the nodes reachable downward from the range's mutation nodes, renumbered in
+ * ascending order (samples keep ids 0..N-1), so the shard is a graph of its own whose node
+ * values take (N + its nodes) x K.  Its triples hold the new node ids and the original mutation
+ * ids, so a shard reads and writes the full-width input and output columns. */
+typedef struct {
+    oracle_graph g;
+    uint64_t* off;
+    uint32_t* adj;
+    triple_t* trip;
+    uint64_t ntrip;
+    uint64_t nedges;
+} oracle_shard;
+
 typedef struct {
     int nshards;
-    uint8_t** active; /* per shard node mask */
-    triple_t** trip;  /* per shard triples */
-    uint64_t* ntrip;
+    oracle_shard* sh;
 } oracle_shards;
 
-/* Split the mutations into `nshards` contiguous id ranges; each shard keeps the nodes
- * reachable downward from its mutation nodes (what saveGRGSubset keeps, serialize.h:147-166).
- * Requires ordered node ids. */
-oracle_shards* oracle_shards_create(const oracle_graph* g, int nshards) {
-    if (!nodes_are_ordered(g) || nshards < 1) return NULL;
-    oracle_shards* s = (oracle_shards*)calloc(1, sizeof(oracle_shards));
-    s->nshards = nshards;
-    s->active = (uint8_t**)calloc(nshards, sizeof(uint8_t*));
-    s->trip = (triple_t**)calloc(nshards, sizeof(triple_t*));
-    s->ntrip = (uint64_t*)calloc(nshards, sizeof(uint64_t));
-    const uint64_t M = g->num_mutations, n = g->num_nodes;
-    for (int sh = 0; sh < nshards; sh++) {
-        const uint64_t m0 = M * sh / nshards, m1 = M * (sh + 1) / nshards;
-        uint8_t* act = (uint8_t*)calloc(n ? n : 1, 1);
-        triple_t* t = (triple_t*)malloc(sizeof(triple_t) * ((m1 - m0) ? (m1 - m0) : 1));
-        uint64_t nt = 0;
-        for (uint64_t m = m0; m < m1; m++) {
-            t[nt].node = g->mut_node[m];
-            t[nt].mut = (uint32_t)m;
-            t[nt].miss = ORACLE_INVALID_NODE;
-            if (t[nt].node != ORACLE_INVALID_NODE) act[t[nt].node] = 1;
-            nt++;
-        }
-        qsort(t, nt, sizeof(triple_t), triple_cmp);
+typedef struct {
+    const oracle_graph* g;
+    oracle_shards* s;
+    int first, last;
+    uint64_t align;
+    int rc;
+} shard_build_job;
+
+/* First mutation of shard sh: M*sh/n rounded to a multiple of `align` (1: no rounding). */
+static uint64_t shard_start(uint64_t M, int sh, int n, uint64_t align) {
+    if (sh >= n) return M;
+    const uint64_t m = M * (uint64_t)sh / (uint64_t)n;
+    const uint64_t r = (m + align / 2) / align * align;
+    return r < M ? r : M;
+}
+
+static void* shard_build_main(void* arg) {
+    shard_build_job* j = (shard_build_job*)arg;
+    const oracle_graph* g = j->g;
+    oracle_shards* s = j->s;
+    const uint64_t M = g->num_mutations, n = g->num_nodes, N = g->num_samples;
+    uint8_t* act = (uint8_t*)malloc(n ? n : 1);
+    uint32_t* newid = (uint32_t*)malloc(sizeof(uint32_t) * (n ? n : 1));
+    if (!act || !newid) {
+        j->rc = -1;
+        free(act);
+        free(newid);
+        return NULL;
+    }
+    for (int sh = j->first; sh < j->last; sh++) {
+        oracle_shard* out = &s->sh[sh];
+        const uint64_t m0 = shard_start(M, sh, s->nshards, j->align), m1 = shard_start(M, sh + 1, s->nshards, j->align);
+        memset(act, 0, n);
+        for (uint64_t m = m0; m < m1; m++)
+            if (g->mut_node[m] != ORACLE_INVALID_NODE) act[g->mut_node[m]] = 1;
+        uint64_t ne = 0;
         for (uint64_t i = n; i > 0; i--) {
             const uint64_t v = i - 1;
             if (!act[v]) continue;
+            ne += g->down_off[v + 1] - g->down_off[v];
             for (uint64_t e = g->down_off[v]; e < g->down_off[v + 1]; e++) act[g->down_adj[e]] = 1;
         }
-        s->active[sh] = act;
-        s->trip[sh] = t;
-        s->ntrip[sh] = nt;
+        uint64_t cnt = 0;
+        for (uint64_t v = 0; v < n; v++)
+            if (v < N || act[v]) newid[v] = (uint32_t)(cnt++);
+        out->off = (uint64_t*)malloc(sizeof(uint64_t) * (cnt + 1));
+        out->adj = (uint32_t*)malloc(sizeof(uint32_t) * (ne ? ne : 1));
+        out->trip = (triple_t*)malloc(sizeof(triple_t) * ((m1 - m0) ? (m1 - m0) : 1));
+        if (!out->off || !out->adj || !out->trip) {
+            j->rc = -1;
+            break;
+        }
+        uint64_t r = 0, e2 = 0;
+        out->off[0] = 0;
+        for (uint64_t v = 0; v < n; v++) {
+            if (!(v < N || act[v])) continue;
+            if (act[v])
+                for (uint64_t e = g->down_off[v]; e < g->down_off[v + 1]; e++) out->adj[e2++] = newid[g->down_adj[e]];
+            out->off[++r] = e2;
+        }
+        uint64_t nt = 0;
+        for (uint64_t m = m0; m < m1; m++) {
+            const uint32_t node = g->mut_node[m];
+            out->trip[nt].node = (node == ORACLE_INVALID_NODE) ? ORACLE_INVALID_NODE : newid[node];
+            out->trip[nt].mut = (uint32_t)m;
+            out->trip[nt].miss = ORACLE_INVALID_NODE;
+            nt++;
+        }
+        qsort(out->trip, nt, sizeof(triple_t), triple_cmp);
+        out->ntrip = nt;
+        out->nedges = ne;
+        out->g.num_nodes = cnt;
+        out->g.num_samples = N;
+        out->g.ploidy = g->ploidy;
+        out->g.num_mutations = M;
+        out->g.down_off = out->off;
+        out->g.down_adj = out->adj;
+        out->g.mut_node = NULL; /* the triples carry the mapping */
+        out->g.miss_node = NULL;
+        out->g.coals = NULL;
     }
-    return s;
+    free(act);
+    free(newid);
+    return NULL;
 }
 
 void oracle_shards_destroy(oracle_shards* s) {
     if (!s) return;
     for (int i = 0; i < s->nshards; i++) {
-        free(s->active[i]);
-        free(s->trip[i]);
+        free(s->sh[i].off);
+        free(s->sh[i].adj);
+        free(s->sh[i].trip);
     }
-    free(s->active);
-    free(s->trip);
-    free(s->ntrip);
+    free(s->sh);
     free(s);
+}
+
+/* Split the mutations into `nshards` contiguous id ranges whose starts are multiples of `align`
+ * (so that ranges of whole windows share no node with children), built on `threads` threads.
+ * Requires ordered node ids. */
+oracle_shards* oracle_shards_create_mt(const oracle_graph* g, int nshards, int threads, uint64_t align) {
+    if (!nodes_are_ordered(g) || nshards < 1) return NULL;
+    if (align < 1) align = 1;
+    if (threads < 1) threads = 1;
+    if (threads > nshards) threads = nshards;
+    oracle_shards* s = (oracle_shards*)calloc(1, sizeof(oracle_shards));
+    s->nshards = nshards;
+    s->sh = (oracle_shard*)calloc(nshards, sizeof(oracle_shard));
+    pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * threads);
+    shard_build_job* jobs = (shard_build_job*)calloc(threads, sizeof(shard_build_job));
+    for (int t = 0; t < threads; t++) {
+        jobs[t].g = g;
+        jobs[t].s = s;
+        jobs[t].first = (int)((int64_t)nshards * t / threads);
+        jobs[t].last = (int)((int64_t)nshards * (t + 1) / threads);
+        jobs[t].align = align;
+        pthread_create(&th[t], NULL, shard_build_main, &jobs[t]);
+    }
+    int rc = 0;
+    for (int t = 0; t < threads; t++) {
+        pthread_join(th[t], NULL);
+        if (jobs[t].rc) rc = jobs[t].rc;
+    }
+    free(th);
+    free(jobs);
+    if (rc) {
+        oracle_shards_destroy(s);
+        return NULL;
+    }
+    return s;
+}
+
+oracle_shards* oracle_shards_create(const oracle_graph* g, int nshards) {
+    return oracle_shards_create_mt(g, nshards, 1, 1);
+}
+
+uint64_t oracle_shard_edges(const oracle_shards* s, int shard) {
+    return (shard >= 0 && shard < s->nshards) ? s->sh[shard].nedges : 0;
+}
+
+uint64_t oracle_shard_nodes(const oracle_shards* s, int shard) {
+    return (shard >= 0 && shard < s->nshards) ? s->sh[shard].g.num_nodes : 0;
 }
 
 static uint64_t dtype_size(int dtype) {
@@ -403,18 +512,28 @@ static uint64_t dtype_size(int dtype) {
     }
 }
 
-/* One thread per shard; DOWN partial outputs are summed into `out` in shard order. Plain
- * numeric dtypes only, no options (the benchmarked configuration). */
-int oracle_matmul_sharded(const oracle_graph* g, const oracle_shards* s, int dtype, const void* in,
-                          uint64_t in_cols, uint64_t rows, int direction, void* out, uint64_t out_cols) {
+static double now_seconds(void) {
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
+
+/* Shards [first, first + count), one thread each; DOWN partial outputs are summed into `out` in
+ * shard order (the time that summation takes goes to *reduce_seconds when it is not NULL); UP
+ * outputs of different shards are disjoint.  Plain numeric dtypes only, no options (the
+ * benchmarked configuration). */
+int oracle_matmul_shard_range(const oracle_graph* g, const oracle_shards* s, int first, int count, int dtype,
+                              const void* in, uint64_t in_cols, uint64_t rows, int direction, void* out,
+                              uint64_t out_cols, double* reduce_seconds) {
     if (dtype == OR_BOOL) return -4;
-    const int ns = s->nshards;
+    if (first < 0 || count < 1 || first + count > s->nshards) return -5;
+    const int ns = count;
     pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * ns);
     shard_job* jobs = (shard_job*)calloc(ns, sizeof(shard_job));
     const uint64_t esz = dtype_size(dtype), outBytes = rows * out_cols * esz;
     for (int i = 0; i < ns; i++) {
         shard_job* j = &jobs[i];
-        j->g = g;
+        j->g = &s->sh[first + i].g;
         j->dtype = dtype;
         j->in = in;
         j->in_cols = in_cols;
@@ -422,9 +541,8 @@ int oracle_matmul_sharded(const oracle_graph* g, const oracle_shards* s, int dty
         j->direction = direction;
         j->out = (direction == OR_DOWN) ? calloc(outBytes ? outBytes : 1, 1) : out;
         j->out_cols = out_cols;
-        j->active = s->active[i];
-        j->trip = s->trip[i];
-        j->ntrip = s->ntrip[i];
+        j->trip = s->sh[first + i].trip;
+        j->ntrip = s->sh[first + i].ntrip;
         pthread_create(&th[i], NULL, shard_main, j);
     }
     int rc = 0;
@@ -433,6 +551,7 @@ int oracle_matmul_sharded(const oracle_graph* g, const oracle_shards* s, int dty
         if (jobs[i].rc) rc = jobs[i].rc;
     }
     if (direction == OR_DOWN) {
+        const double t0 = now_seconds();
         const uint64_t cnt = rows * out_cols;
         for (int i = 0; i < ns; i++) {
 #define SUMINTO(T)                                                       \
@@ -452,8 +571,17 @@ int oracle_matmul_sharded(const oracle_graph* g, const oracle_shards* s, int dty
 #undef SUMINTO
             free(jobs[i].out);
         }
+        if (reduce_seconds) *reduce_seconds = now_seconds() - t0;
+    } else if (reduce_seconds) {
+        *reduce_seconds = 0.0;
     }
     free(th);
     free(jobs);
     return rc;
+}
+
+/* Every shard, one thread each (the reference's all-cores pattern). */
+int oracle_matmul_sharded(const oracle_graph* g, const oracle_shards* s, int dtype, const void* in,
+                          uint64_t in_cols, uint64_t rows, int direction, void* out, uint64_t out_cols) {
+    return oracle_matmul_shard_range(g, s, 0, s->nshards, dtype, in, in_cols, rows, direction, out, out_cols, NULL);
 }

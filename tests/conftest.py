@@ -91,3 +91,29 @@ def assert_matches(got, ref, scale=None, rtol=None):
     bound = rtol * scale.astype(np.float64) + 1e-300
     bad = np.flatnonzero(err.ravel() > bound.ravel())
     assert bad.size == 0, f"{bad.size} outputs beyond rtol={rtol}: max err/scale {np.max(err / np.maximum(scale, 1e-300))}"
+
+
+def oracle_graph_of(g):
+    """The oracle's view of a grgl_gb300 graph (its exported CSR arrays)."""
+    import oracle
+
+    a = g.export_arrays()
+    return oracle.OracleGraph(num_samples=g.num_samples, ploidy=g.ploidy, down_off=a["down_off"],
+                              down_adj=a["down_adj"], mut_node=a["mut_node"])
+
+
+def assert_matches_oracle(og, V, direction, got, by_individual=False):
+    """`got` against the oracle on the same input: integers bit-exact; float64 within 1e-12 and
+    (compensated) float32 within 1e-6 of the sum of |terms| per output, float32 against the
+    oracle's float64 product of the same inputs."""
+    import oracle
+
+    V = np.asarray(V)
+    got = np.asarray(got)
+    if V.dtype.kind != "f":
+        assert_matches(got, oracle.matmul(og, V, direction, by_individual=by_individual))
+        return
+    V64 = V.astype(np.float64)
+    ref = oracle.matmul(og, V64, direction, by_individual=by_individual)
+    scale = oracle.matmul(og, np.abs(V64), direction, by_individual=by_individual)
+    assert_matches(got.astype(np.float64), ref, scale, rtol=1e-6 if V.dtype == np.float32 else 1e-12)

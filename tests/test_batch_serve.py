@@ -5,7 +5,7 @@ import threading
 import numpy as np
 import pytest
 
-from tests.conftest import assert_matches
+from tests.conftest import assert_matches, assert_matches_oracle, oracle_graph_of
 
 pytestmark = pytest.mark.gpu
 DOWN, UP = 1, 2
@@ -21,6 +21,11 @@ def gx(cuda_ok):
 @pytest.fixture(scope="module")
 def graphs(gx):
     return gx.window_tree_grg(2000, 20000, seed=31).upload(), gx.window_tree_grg(500, 3000, seed=32).upload()
+
+
+@pytest.fixture(scope="module")
+def oracles(graphs):
+    return [oracle_graph_of(g) for g in graphs]
 
 
 def _rand(rng, dtype, shape):
@@ -39,7 +44,7 @@ def _check_same(gx, g, V, d, got):
         assert_matches(got, ref)
 
 
-def test_matmul_batch_matches_single(gx, graphs):
+def test_matmul_batch_matches_single(gx, graphs, oracles):
     g = graphs[0]
     rng = np.random.default_rng(0)
     reqs = []
@@ -51,6 +56,12 @@ def test_matmul_batch_matches_single(gx, graphs):
     outs = gx.matmul_batch(g, reqs)
     for (V, d), out in zip(reqs, outs):
         _check_same(gx, g, V, d, out)
+    # one request per dtype and direction against the oracle as well
+    seen = set()
+    for (V, d), out in zip(reqs, outs):
+        if (V.dtype, d) not in seen:
+            seen.add((V.dtype, d))
+            assert_matches_oracle(oracles[0], V, d, out)
     # a tiny stacking width forces many traversals; device tensors take the device path
     import torch
 
@@ -60,7 +71,7 @@ def test_matmul_batch_matches_single(gx, graphs):
         _check_same(gx, g, V, d, out.cpu().numpy())
 
 
-def test_server_results_alone_and_in_the_mix(gx, graphs):
+def test_server_results_alone_and_in_the_mix(gx, graphs, oracles):
     rng = np.random.default_rng(1)
     reqs = []
     for i in range(40):
@@ -91,11 +102,15 @@ def test_server_results_alone_and_in_the_mix(gx, graphs):
         for t in th:
             t.join()
         batched = 0
+        seen = set()
         for i, (gid, V, d) in enumerate(reqs):
             out, st = srv.result(tickets[i], timeout=120)
             batched += st["batch_requests"] > 1
             assert st["done_s"] >= st["start_s"] >= st["submit_s"]
             _check_same(gx, graphs[gid], V, d, out)
+            if (gid, V.dtype) not in seen:  # one served result per graph and dtype vs the oracle
+                seen.add((gid, V.dtype))
+                assert_matches_oracle(oracles[gid], V, d, out)
         assert batched > 0  # queued requests were coalesced
 
 

@@ -122,6 +122,45 @@ def test_sharded_oracle_matches_plain():
         assert np.array_equal(sh.matmul(V, direction), oracle.matmul(g, V, direction))
 
 
+def test_sharded_oracle_ranges_and_alignment():
+    """Window-aligned ranged shards: every edge belongs to exactly one shard, a run over a range of
+    shards equals the sum (DOWN) / the columns (UP) of its shards, and the whole set equals the
+    plain product."""
+    g = oracle.window_tree(300, 2500, seed=4, threads=3)
+    sh = oracle.Shards(g, 7, build_threads=3, align=100)
+    assert sh.edges() == g.num_edges
+    rng = np.random.default_rng(6)
+    V = rng.integers(-9, 9, size=(2, g.num_mutations)).astype(np.int64)
+    parts = [sh.matmul(V, DOWN, first=i, count=1) for i in range(7)]
+    assert np.array_equal(sum(parts), oracle.matmul(g, V, DOWN))
+    assert np.array_equal(sh.matmul(V, DOWN, first=2, count=3), parts[2] + parts[3] + parts[4])
+    U = rng.integers(-9, 9, size=(2, g.num_samples)).astype(np.int32)
+    assert np.array_equal(sh.matmul(U, UP), oracle.matmul(g, U, UP))
+
+
+@pytest.mark.parametrize("N,M,seed", [(2, 5, 1), (777, 1234, 5), (1000, 10000, 42)])
+def test_oracle_generator_equals_product_generator(N, M, seed):
+    """The oracle's own window-tree generator (window_tree.c) and the product's build the same
+    graph bit for bit; the CPU reference arm of the benchmark relies on it."""
+    gx = pytest.importorskip("grgl_gb300")
+    og = oracle.window_tree(N, M, seed=seed, threads=2)
+    a = gx.window_tree_grg(N, M, seed=seed).export_arrays()
+    assert np.array_equal(og.down_off, a["down_off"])
+    assert np.array_equal(og.down_adj, a["down_adj"])
+    assert np.array_equal(og.mut_node, a["mut_node"])
+
+
+def test_oracle_generator_matches_golden_window_tree():
+    """The N=1,000 / M=10,000 seed-42 window-tree genotypes (the golden fixture was built from them
+    by the reference constructor): same allele counts from both graphs."""
+    from tests.conftest import GOLDEN
+
+    og = oracle.window_tree(1000, 10000, seed=42)
+    ref = oracle.read_grg(GOLDEN / "wt_n1000_m10000.grg")
+    ones = np.ones((1, 1000), dtype=np.int64)
+    assert np.array_equal(oracle.matmul(og, ones, UP), oracle.matmul(ref, ones, UP))
+
+
 def test_read_grg_missing_nodes():
     from tests.conftest import GOLDEN
 

@@ -91,6 +91,28 @@ def _rank_main(rank, world, port, result_dir):
     down = shard.distributed_matmul(shards, ranges, owned, Vd, DOWN, g.num_samples, g.num_mutations, _oracle_fn)
     np.save(os.path.join(result_dir, f"up{rank}.npy"), up)
     np.save(os.path.join(result_dir, f"down{rank}.npy"), down)
+    # the device-tensor form (the one nccl runs), here on host tensors under gloo
+    import torch
+
+    def tensor_fn(s, X, d):
+        return torch.from_numpy(_oracle_fn(s, X.numpy(), d))
+
+    downt = shard.distributed_matmul(shards, ranges, owned, torch.from_numpy(Vd), DOWN, g.num_samples,
+                                     g.num_mutations, tensor_fn)
+    assert isinstance(downt, torch.Tensor)
+    np.save(os.path.join(result_dir, f"downt{rank}.npy"), downt.numpy())
+    # GF(2): partials from different ranks combine by XOR, not OR
+    Vb = rng.integers(0, 2, size=(3, g.num_mutations)).astype(bool)
+    bd = shard.distributed_matmul(shards, ranges, owned, Vb, DOWN, g.num_samples, g.num_mutations, _oracle_fn)
+    np.save(os.path.join(result_dir, f"bool{rank}.npy"), bd)
+    # one range per rank, combined by combine_rank_output (the benchmark's multi-GPU step)
+    r2 = shard.mutation_ranges(g, world, align=100)
+    mine = g.subset_mutations(np.arange(r2[rank].start, r2[rank].stop, dtype=np.uint32))
+    upr = shard.combine_rank_output(torch.from_numpy(_oracle_fn(mine, Vu, UP)), UP, r2)
+    dnr = shard.combine_rank_output(
+        torch.from_numpy(_oracle_fn(mine, np.ascontiguousarray(Vd[:, r2[rank].start:r2[rank].stop]), DOWN)), DOWN, r2)
+    np.save(os.path.join(result_dir, f"upr{rank}.npy"), upr.numpy())
+    np.save(os.path.join(result_dir, f"dnr{rank}.npy"), dnr.numpy())
     dist.destroy_process_group()
 
 
@@ -108,9 +130,18 @@ def test_distributed_combine_gloo(graph, tmp_path):
     Vd = rng.standard_normal((2, g.num_mutations))
     ref_up, ref_down = oracle.matmul(full, Vu, UP), oracle.matmul(full, Vd, DOWN)
     scale = oracle.matmul(full, np.abs(Vd), DOWN)
+    Vb = np.random.default_rng(5)
+    Vb.integers(-20, 20, size=(2, g.num_samples))
+    Vb.standard_normal((2, g.num_mutations))
+    Vb = Vb.integers(0, 2, size=(3, g.num_mutations)).astype(bool)
+    ref_bool = oracle.matmul(full, Vb, DOWN)
     for r in range(world):
         assert np.array_equal(np.load(tmp_path / f"up{r}.npy"), ref_up)
         assert np.all(np.abs(np.load(tmp_path / f"down{r}.npy") - ref_down) <= 1e-12 * scale)
+        assert np.all(np.abs(np.load(tmp_path / f"downt{r}.npy") - ref_down) <= 1e-12 * scale)
+        assert np.array_equal(np.load(tmp_path / f"bool{r}.npy"), ref_bool)
+        assert np.array_equal(np.load(tmp_path / f"upr{r}.npy"), ref_up)
+        assert np.all(np.abs(np.load(tmp_path / f"dnr{r}.npy") - ref_down) <= 1e-12 * scale)
 
 
 @pytest.mark.gpu
