@@ -42,8 +42,8 @@ def parse_args():
     ap.add_argument("--seed", type=int, default=42)
     ap.add_argument("--ks", default="1,8,32,64")
     ap.add_argument("--dtypes", default="int32,float32,float64")
-    ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline sample budget")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-parity", action="store_true", help="skip the full-size comparison with the oracle")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end pass")
     ap.add_argument("--e2e-streams", type=int, default=4,
                     help="CUDA streams the end-to-end pass spreads the step's calls over")
@@ -146,37 +146,72 @@ class Clocks:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def cpu_baseline(args, combos, seconds_budget, threads=None):
-    """The oracle port (the reference's range-split multi-core pattern) on a bounded sample of the
-    workload: the same generator with a prefix of the variants."""
-    import grgl_gb300 as gx
-    import oracle
+def workload_config(args, combos, stats):
+    """The `config` object of both arms' lines: the workload and the graph it runs on."""
+    return {"workload": workload_name(args, combos),
+            "graph": {k: stats[k] for k in ("samples", "mutations", "nodes", "edges")},
+            "l2": "inputs larger than L2 (the 8 GB edge CSR is streamed by every traversal)"}
 
-    oracle.build()
-    threads = threads or os.cpu_count() or 1
-    # size the sample: ~1.5e8 edge*K per core-second for the sharded restatement (probe below)
-    sample_m = max(1000, min(args.mutations, 20000))
-    g = gx.window_tree_grg(args.samples, sample_m, seed=args.seed)
-    a = g.export_arrays()
-    og = oracle.OracleGraph(num_samples=args.samples, ploidy=2, down_off=a["down_off"], down_adj=a["down_adj"],
-                            mut_node=a["mut_node"])
-    sh = oracle.Shards(og, threads)
-    rng = np.random.default_rng(1)
-    E = og.num_edges
-    total_units, total_t = 0, 0.0
-    t_start = time.perf_counter()
-    for dt, K, d in combos:
-        V = make_inputs(rng, [(dt, K, d)], og.num_samples, og.num_mutations)[0]
+
+class CpuSampler:
+    """The reference CPU matmul (the oracle's restatement of GRG::matrixMultiplication,
+    grg.h:1341-1517) run the way the reference runs on many cores: the graph cut into one
+    window-aligned mutation range per core, each range's sub-graph (every sample and the nodes
+    below the range, what saveGRGSubset keeps) multiplied on its own thread, DOWN partial outputs
+    summed (test/endtoend/test_matmul.py:264-325).  Every product covers the whole graph."""
+
+    def __init__(self, og, combos, inputs, threads):
+        import oracle
+
+        self.combos, self.inputs = combos, inputs
+        self.threads = threads
+        self.edges = og.num_edges
         t0 = time.perf_counter()
-        sh.matmul(V, d)
-        total_t += time.perf_counter() - t0
-        total_units += E * K
-        if time.perf_counter() - t_start > seconds_budget:
-            break
-    return {"value": total_units / total_t, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"window-tree N={args.samples} M={sample_m} (E={E}); "
-                      f"{'all' if time.perf_counter() - t_start <= seconds_budget else 'first'} workload combos; "
-                      f"{total_units:.3g} edge*K in {total_t:.1f}s"}
+        self.sh = oracle.Shards(og, threads, build_threads=threads, align=100)
+        self.build_s = time.perf_counter() - t0
+
+    def run(self, idxs):
+        """The combos `idxs` over the whole graph: (edge*K units, seconds, DOWN partial-sum seconds)."""
+        units, secs, red = 0, 0.0, 0.0
+        for i in idxs:
+            (dt, K, d), V = self.combos[i], self.inputs[i]
+            t0 = time.perf_counter()
+            self.sh.matmul(V, d)
+            secs += time.perf_counter() - t0
+            red += self.sh.last_reduce_s
+            units += self.edges * K
+        return units, secs, red
+
+    def one_core(self):
+        """One thread on one range (the reference as shipped: a single-threaded call), for every
+        combo with K in {1, 8}."""
+        out = {}
+        e0 = self.sh.edges(0, 1)
+        for (dt, K, d), V in zip(self.combos, self.inputs):
+            if K not in (1, 8):
+                continue
+            t0 = time.perf_counter()
+            self.sh.matmul(V, d, first=0, count=1)
+            out[f"{dt.name}:{K}:{'UP' if d == UP else 'DOWN'}"] = e0 * K / (time.perf_counter() - t0)
+        return out
+
+
+def step_plan(n_combos, steps):
+    """Combo indices per timed step: every combo exactly once over the steps when steps <= n
+    (consecutive groups), one combo per step, cycling, when steps > n."""
+    if steps >= n_combos:
+        return [[s % n_combos] for s in range(steps)]
+    return [list(range(n_combos * s // steps, n_combos * (s + 1) // steps)) for s in range(steps)]
+
+
+def cpu_baseline(args, combos, smp):
+    """The CPU reference on the box's cores over a bounded sample of the workload: the K in {1, 8}
+    combos, each over the whole graph."""
+    idxs = [i for i, (_, K, _) in enumerate(combos) if K in (1, 8)] or [0]
+    units, secs, _ = smp.run(idxs)
+    return {"value": units / secs, "unit": UNIT, "cores": smp.threads, "kind": "port",
+            "sample": f"the {len(idxs)} K in {{1, 8}} combos of the workload, each over the whole benchmark graph "
+                      f"(one window-aligned mutation range per core); {units:.3g} edge*K in {secs:.1f} s"}
 
 
 def batched_vs_plain(gx, torch, g, E, rng, n_req, kmax, label, std_every=0, err_sample=0):
@@ -355,12 +390,14 @@ def cold_start(gx, torch, g):
             os.unlink(path)
 
 
-def large_graph(gx, torch, args, peak):
+def large_graph(gx, torch, args, l2_peak):
     """The large window-tree graph (N=1,000,000 haplotypes, a variant prefix sized to 2-4e9 edges):
     float32 compensated and float64 at K in {16, 64, 256}, both directions, device inputs.  Each
-    entry: sweep device time (CUDA events), edge*K/s, algorithmic GB/s against the HBM peak, and the
-    float32 result's max error against the float64 result, relative to the sum of |terms| per
-    output (|V| X); the float64 result is checked against native FP64 accumulation at K=16."""
+    entry: sweep device time (CUDA events), edge*K/s, gathered GB/s (edge ids + one row per edge)
+    against the L2 read ceiling measured in this run, and the float32 result's max error against
+    the float64 result, relative to the sum of |terms| per output (|V| X); the float64 result is
+    checked against native FP64 accumulation at K=16.  Then float32 and float64 K=16 products in
+    both directions against the oracle (all host cores) on this graph.""" 
     t0 = time.perf_counter()
     g = gx.window_tree_grg(args.large_samples, args.large_mutations, seed=args.seed)
     t_gen = time.perf_counter() - t0
@@ -393,11 +430,11 @@ def large_graph(gx, torch, args, peak):
                     res = gx.matmul(g, V, d)
                 t = gx.last_timing()
                 s = V.element_size()
+                gath = E * (4 + K * s) / (t["sweep_ms"] / 1e3) / 1e9
                 rows.append({"dtype": "float64" if s == 8 else "float32", "K": K, "dir": "UP" if d == UP else "DOWN",
                              "sweep_ms": t["sweep_ms"], "total_ms": t["total_ms"],
                              "edgeK_per_s": E * K / (t["sweep_ms"] / 1e3),
-                             "alg_GBps": alg_bytes(stats, K, s, d) / (t["sweep_ms"] / 1e3) / 1e9,
-                             "hbm_frac": alg_bytes(stats, K, s, d) / (t["sweep_ms"] / 1e3) / 1e9 / peak})
+                             "gathered_GBps": gath, "l2_frac": gath / l2_peak})
                 if s == 8:
                     y64 = res
                 else:
@@ -411,8 +448,7 @@ def large_graph(gx, torch, args, peak):
     gx.set_timing(False)
     units = sum(E * r["K"] for r in rows)
     secs = sum(r["sweep_ms"] for r in rows) / 1e3
-    abytes = sum(alg_bytes(stats, r["K"], 8 if r["dtype"] == "float64" else 4, UP if r["dir"] == "UP" else DOWN)
-                 for r in rows)
+    gbytes = sum(E * (4 + r["K"] * (8 if r["dtype"] == "float64" else 4)) for r in rows)
     # a batched mix on the same graph: 64 requests, K ~ U{1..128}, UP/DOWN 50/50, compensated
     # float32, stacked into shared traversals (wall clock around the whole batch)
     reqs = []
@@ -428,41 +464,164 @@ def large_graph(gx, torch, args, peak):
     torch.cuda.synchronize()
     t_b = time.perf_counter() - t0
     b_units = sum(E * V.shape[0] for V, _ in reqs)
-    b_bytes = sum(alg_bytes(stats, V.shape[0], 4, d) for V, d in reqs)
+    b_bytes = sum(E * (4 + 4 * V.shape[0]) for V, _ in reqs)
     batched = {"requests": len(reqs), "columns": int(sum(V.shape[0] for V, _ in reqs)), "seconds": t_b,
-               "edgeK_per_s": b_units / t_b, "alg_GBps": b_bytes / t_b / 1e9, "hbm_frac": b_bytes / t_b / 1e9 / peak,
+               "edgeK_per_s": b_units / t_b, "gathered_GBps": b_bytes / t_b / 1e9,
+               "l2_frac": b_bytes / t_b / 1e9 / l2_peak,
                "mix": "K~U{1..128}, UP/DOWN 50/50, float32 compensated, device inputs"}
     del reqs
     # and served: Poisson arrivals at 1000 req/s, the serving mix, on this graph alone
     serve = served(gx, [g], 1000.0, 1.0, 48, rng)
+    parity = None
+    if not args.no_parity:
+        og = oracle_graph(g)
+        parity = parity_vs_oracle(gx, torch, g, og, [(np.float32, 16, UP), (np.float32, 16, DOWN),
+                                                     (np.float64, 16, UP), (np.float64, 16, DOWN)], seed=17)
+        parity["graph"] = "this graph (UP runs in split form above 2^31 edges)"
+        del og
     del g
     torch.cuda.empty_cache()
     return {"graph": dict(stats, note=f"variant prefix M'={args.large_mutations} of the 10,000,000-variant "
                                       "generator run, sized to the 2-4e9-edge budget"),
-            "edgeK_per_s": units / secs, "alg_GBps": abytes / secs / 1e9, "hbm_frac": abytes / secs / 1e9 / peak,
-            "matmuls": rows, "batched": batched, "served": serve,
+            "edgeK_per_s": units / secs, "gathered_GBps": gbytes / secs / 1e9, "l2_frac": gbytes / secs / 1e9 / l2_peak,
+            "matmuls": rows, "batched": batched, "served": serve, "parity_vs_oracle": parity,
             "setup_s": {"generate": t_gen, "plan_upload": t_up, "autotune": t_tune}}
 
 
+def native_libraries():
+    """Shared libraries of this repository mapped into the process (Linux /proc/self/maps)."""
+    try:
+        maps = Path("/proc/self/maps").read_text().splitlines()
+    except OSError:
+        return None
+    root = str(ROOT)
+    return sorted({ln.split()[-1][len(root) + 1:] for ln in maps
+                   if ln.split()[-1].startswith(root) and ".so" in ln.split()[-1]})
+
+
 def run_reference(args):
+    """The reference arm: the reference's CPU matmul (the oracle's restatement, compiled on this
+    host) on all the host cores, the reference's range-split pattern, on the same graph, inputs,
+    combos and config as the GPU arm.  The timed steps cover every combo of the workload once,
+    each over the whole graph (step_plan).  The process loads only the oracle library: the graph
+    comes from the oracle's own generator (window_tree.c, the same graph bit for bit)."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
+    import oracle
+
+    oracle.build()
     combos = workload(args)
-    budget = max(5.0, args.cpu_seconds)
-    vals = []
-    cb = None
-    for _ in range(args.warmup + args.steps):
-        cb = cpu_baseline(args, combos, budget / max(1, args.steps))
-        vals.append(cb["value"])
-    v = statistics.median(vals[args.warmup:]) if len(vals) > args.warmup else vals[-1]
+    threads = oracle.host_threads()
+    t0 = time.perf_counter()
+    og = oracle.window_tree(args.samples, args.mutations, seed=args.seed, threads=threads)
+    t_gen = time.perf_counter() - t0
+    stats = {"samples": og.num_samples, "mutations": og.num_mutations, "nodes": og.num_nodes, "edges": og.num_edges}
+    inputs = make_inputs(np.random.default_rng(7), combos, og.num_samples, og.num_mutations)
+    smp = CpuSampler(og, combos, inputs, threads)
+    del og  # the shards hold their own sub-graphs
+    k1 = [i for i, (_, K, _) in enumerate(combos) if K == 1] or [0]
+    for s in range(args.warmup):  # warm-up steps: the single-vector combos
+        smp.run([k1[s % len(k1)]])
+    plan = step_plan(len(combos), args.steps)
+    units, secs, red, per_step = 0, 0.0, 0.0, []
+    for idxs in plan:
+        u, t, r = smp.run(idxs)
+        units += u
+        secs += t
+        red += r
+        per_step.append(t)
+    v = units / secs
+    one = smp.one_core()
+    passes = sum(len(x) for x in plan) / len(combos)
+    cb = {"value": v, "unit": UNIT, "cores": smp.threads, "kind": "port",
+          "sample": f"the whole workload: each of the {len(combos)} combos over the whole graph "
+                    f"({passes:.2f} passes over the combos in the {args.steps} timed steps; {units:.3g} edge*K in "
+                    f"{secs:.1f} s)"}
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "int32,float32,float64", "data": "synthetic (seeded window-tree GRG)", "impl": "reference",
-            "config": {"workload": workload_name(args, combos)},
-            "cpu_baseline": dict(cb, value=v),
-            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int32,float32,float64",
+            "data": "synthetic (seeded window-tree GRG)", "impl": "reference",
+            "config": workload_config(args, combos, stats),
+            "cpu_baseline": cb,
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "reference_cpu": {
+                "what": "the reference CPU GRG::matrixMultiplication (grg.h:1341-1517) as restated by the oracle "
+                        "(grg_oracle.c, gcc -O3, loop for loop), run with the reference's own multi-core pattern",
+                "timed_passes_over_combos": passes,
+                "all_cores": {"cores": smp.threads, "edgeK_per_s": v,
+                              "timed_steps_ms": [round(1e3 * t, 1) for t in per_step],
+                              "combos_per_step": [len(x) for x in plan]},
+                "one_core": {"edgeK_per_s": one, "mean_edgeK_per_s": statistics.fmean(one.values()) if one else None,
+                             "what": "one thread, one call over one range (1/cores of the graph): the reference "
+                                     "as shipped"},
+                "split_overhead": {"range_build_s": smp.build_s,
+                                   "down_partial_sum_s_per_step": red / args.steps,
+                                   "down_partial_sum_share": red / secs,
+                                   "what": "building the mutation ranges' sub-graphs (once) and summing DOWN partial "
+                                           "outputs (inside the timed steps)"},
+                "setup_s": {"generate": t_gen},
+                "native_libraries": native_libraries(),
+            }}
     print(json.dumps(line), flush=True)
+
+
+def parity_vs_oracle(gx, torch, g, og, checks, seed, shards=None):
+    """GPU products of `g` against the oracle (the reference algorithm, all host cores, sharded)
+    on the same seeded inputs: integers bit-exact; floats against the oracle's float64 product,
+    per output, relative to the sum of |terms| (the tolerance's scale) and to |output|."""
+    import oracle
+
+    sh = shards or oracle.Shards(og, oracle.host_threads(), align=100)
+    rng = np.random.default_rng(seed)
+    N, M = g.num_samples, g.num_mutations
+    rows = []
+    t_all = time.perf_counter()
+    for dt, K, d in checks:
+        dt = np.dtype(dt)
+        cols = N if d == UP else M
+        if dt.kind == "f":
+            V = rng.standard_normal((K, cols)).astype(dt)
+        else:
+            V = rng.integers(0, 2, size=(K, cols)).astype(dt)  # 0/1 genotype rows; the first is all ones
+            V[0] = 1
+        got = gx.matmul(g, torch.from_numpy(V).cuda(), d)
+        torch.cuda.synchronize()
+        got = got.cpu().numpy()
+        rec = {"dtype": dt.name, "K": K, "dir": "UP" if d == UP else "DOWN", "outputs": int(got.size)}
+        if dt.kind != "f":
+            ref = sh.matmul(V, d)
+            mism = int(np.count_nonzero(got != ref))
+            rec.update({"bit_exact": mism == 0, "mismatches": mism})
+        else:
+            V64 = V.astype(np.float64)
+            ref = sh.matmul(V64, d)
+            scale = sh.matmul(np.abs(V64), d)
+            err = np.abs(got.astype(np.float64) - ref)
+            tol = 1e-6 if dt == np.float32 else 1e-12
+            nz = np.abs(ref) > 0
+            rec.update({"max_err_rel_sum_abs_terms": float(np.max(err / np.maximum(scale, 1e-300))),
+                        "max_err_rel_output": float(np.max(err[nz] / np.abs(ref[nz]))) if nz.any() else 0.0,
+                        "median_err_rel_output": float(np.median(err[nz] / np.abs(ref[nz]))) if nz.any() else 0.0,
+                        "tolerance_rel_sum_abs_terms": tol,
+                        "within_tolerance": bool(np.all(err <= tol * scale + 1e-300)),
+                        "reference": "oracle float64 on the same inputs"})
+        rows.append(rec)
+    return {"checks": rows, "oracle_threads": sh.nshards, "seconds": time.perf_counter() - t_all,
+            "all_pass": all(r.get("bit_exact", r.get("within_tolerance")) for r in rows)}
+
+
+def oracle_graph(g):
+    import oracle
+
+    a = g.export_arrays()
+    return oracle.OracleGraph(num_samples=g.num_samples, ploidy=g.ploidy, down_off=a["down_off"],
+                              down_adj=a["down_adj"], mut_node=a["mut_node"])
+
+
+def load_peaks():
+    pk = ROOT / "MEASURED_PEAKS.json"
+    return json.loads(pk.read_text()) if pk.exists() else {}
 
 
 def main():
@@ -482,18 +641,35 @@ def main():
         dist.init_process_group("nccl")
     combos = workload(args)
     t0 = time.perf_counter()
-    g = gx.window_tree_grg(args.samples, args.mutations, seed=args.seed + rank)
+    full = gx.window_tree_grg(args.samples, args.mutations, seed=args.seed)
     t_gen = time.perf_counter() - t0
-    stats = graph_stats(g)
+    stats = graph_stats(full)
+    # N > 1: range shards of the one graph (the reference's split pattern, serialize.h:147-166):
+    # rank r keeps mutation range r (whole windows), DOWN partial outputs are all-reduced and UP
+    # column blocks all-gathered over NCCL
+    my_range = range(0, stats["mutations"])
+    ranges = [my_range]
+    g = full
+    if world > 1:
+        from grgl_gb300 import shard
+
+        ranges = shard.mutation_ranges(full, world, align=100)
+        assert len(ranges) == world, "fewer window-aligned ranges than ranks"
+        my_range = ranges[rank]
+        g = full.subset_mutations(np.arange(my_range.start, my_range.stop, dtype=np.uint32))
     t0 = time.perf_counter()
     g.upload()
     torch.cuda.synchronize()
     t_up = time.perf_counter() - t0
-    stats["levels"] = g.info()["num_levels"]
-    stats["device_bytes"] = g.info()["device_bytes"]
+    shard_stats = graph_stats(g)
+    levels = g.info()["num_levels"]
+    device_bytes = g.info()["device_bytes"]
     rng = np.random.default_rng(7)
     host_inputs = make_inputs(rng, combos, stats["samples"], stats["mutations"])
     dev_inputs = [torch.from_numpy(V).cuda() for V in host_inputs]
+    if world > 1:  # DOWN reads only this rank's mutation columns
+        dev_inputs = [V if d == UP else V[:, my_range.start:my_range.stop].contiguous()
+                      for (_, _, d), V in zip(combos, dev_inputs)]
     torch.cuda.synchronize()
 
     def barrier():
@@ -501,17 +677,23 @@ def main():
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
+    def combine(out, d):
+        if world == 1:
+            return out
+        from grgl_gb300 import shard
+
+        return shard.combine_rank_output(out, d, ranges)
+
     def step(inputs, record):
         for (dt, K, d), V in zip(combos, inputs):
-            gx.matmul(g, V, d)
+            combine(gx.matmul(g, V, d), d)
             if record is not None:
-                t = gx.last_timing()
-                record.append((dt, K, d, t))
+                record.append((dt, K, d, gx.last_timing()))
 
     if args.breakdown:
         gx.set_timing(True)
-        E = stats["edges"]
-        print(json.dumps({"graph": stats}), flush=True)
+        E = shard_stats["edges"]
+        print(json.dumps({"graph": shard_stats}), flush=True)
         for (dt, K, d), V in zip(combos, dev_inputs):
             for _ in range(3):
                 gx.matmul(g, V, d)
@@ -564,8 +746,9 @@ def main():
     if world > 1:
         torch.distributed.all_reduce(ms_t, op=torch.distributed.ReduceOp.MAX)
     ms = float(ms_t.item())
+    # the whole job's work: every edge of the one graph, K updates each, per matmul
     units_per_step = sum(stats["edges"] * K for _, K, _ in combos)
-    value = units_per_step * args.steps * world / (ms / 1000.0)
+    value = units_per_step * args.steps / (ms / 1000.0)
 
     if tune is not None:
         # the same step on the default shapes, for the tuner's gain (untimed for `value`)
@@ -580,35 +763,71 @@ def main():
         tune["sweep_ms_per_step_default_shapes"] = sum(t["sweep_ms"] for *_, t in recs)
         tune["sweep_ms_per_step_tuned"] = sum(t["sweep_ms"] for *_, t in records) / args.steps
 
-    # roofline of the sweep kernel over the timed region
+    # ---- ceilings of the sweep kernel over the timed region -----------------------------------
+    # The gathers are served by L2 (the node rows a level gathers are reused across its warps),
+    # so the bound is L2 read bandwidth: edge ids + one gathered row per edge, per launch, against
+    # the L2 -> SM read bandwidth measured in this run.  Beside it, the DRAM bytes ncu counts
+    # (a capture of the same step on a quarter-size graph, scaled by edges) against the HBM peak.
+    E = shard_stats["edges"]
     sweep_ms = sum(t["sweep_ms"] for *_, t in records)
-    abytes = sum(alg_bytes(stats, K, dt.itemsize, d) for dt, K, d, _ in records)
-    compulsory = sum(stats["edges"] * 4 + (stats["nodes"] + 1) * 8 + 2 * stats["nodes"] * K * dt.itemsize
-                     for dt, K, d, _ in records)
+    sweep_s_step = sweep_ms / args.steps / 1e3
     launches = sum(t["launches"] for *_, t in records)
-    # the gathers' own ceiling: edge ids + one row per edge, against the measured L2 -> SM bandwidth
-    gathered = sum(stats["edges"] * (4 + K * dt.itemsize) for dt, K, d, _ in records)
+    gathered = sum(E * (4 + K * dt.itemsize) for dt, K, d, _ in records) / args.steps
+    abytes = sum(alg_bytes(shard_stats, K, dt.itemsize, d) for dt, K, d, _ in records) / args.steps
+    compulsory = sum(E * 4 + (shard_stats["nodes"] + 1) * 8 + 2 * shard_stats["nodes"] * K * dt.itemsize
+                     for dt, K, d, _ in records) / args.steps
     l2_peak = gx.measure_l2_bandwidth()
-    peaks = {}
-    pk = ROOT / "MEASURED_PEAKS.json"
-    if pk.exists():
-        peaks = json.loads(pk.read_text())
-    peak = peaks.get("hbm_gbs", 6800.0)
-    achieved = abytes / (sweep_ms / 1000.0) / 1e9
-    traffic = None
+    peaks = load_peaks()
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    hbm_src = "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in peaks else "fallback 6800 GB/s (of fallback)"
+    traffic = traffic_src = None
     tfile = ROOT / "profiles" / "sweep_traffic.json"
-    default_step = (not args.only and args.samples == 200_000 and args.mutations == 1_000_000
+    default_step = (world == 1 and not args.only and args.samples == 200_000 and args.mutations == 1_000_000
                     and args.ks == "1,8,32,64" and args.dtypes == "int32,float32,float64")
     if tfile.exists() and default_step:
-        traffic = json.loads(tfile.read_text()).get("bytes_per_step")
+        tf = json.loads(tfile.read_text())
+        if tf.get("dram_bytes_per_step") and tf.get("graph", {}).get("edges"):
+            traffic = tf["dram_bytes_per_step"] * E / tf["graph"]["edges"]
+            traffic_src = (f"ncu dram__bytes_read.sum + dram__bytes_write.sum over every sweep launch of one step on "
+                           f"the N={tf['graph']['samples']}, M={tf['graph']['mutations']} graph "
+                           f"(E={tf['graph']['edges']}), scaled by edges x{E / tf['graph']['edges']:.2f} "
+                           "(profiles/sweep_traffic.json)")
+    k1 = [(dt, d, t["sweep_ms"]) for dt, K, d, t in records if K == 1]
+    id_stream = None
+    if k1:
+        rates = [E * 4 / (ms_ / 1e3) / 1e9 for _, _, ms_ in k1]
+        id_stream = {"achieved": statistics.fmean(rates), "peak": hbm_peak, "unit": "GB/s",
+                     "frac": statistics.fmean(rates) / hbm_peak,
+                     "what": "K=1 matmuls: the 4-byte edge-id stream (E x 4 bytes, read once from HBM) / sweep "
+                             "time; the part of the step HBM itself bounds"}
+    roofline = {
+        "bound": "l2", "kernel": "grgx::sweep_kernel",
+        "achieved": gathered / sweep_s_step / 1e9, "peak": l2_peak, "unit": "GB/s",
+        "frac": gathered / sweep_s_step / 1e9 / l2_peak,
+        "traffic": traffic, "traffic_source": traffic_src,
+        "what": "edge ids + one gathered row per edge (E x (4 + K x s) bytes per matmul) over the step's sweep "
+                "launches / their CUDA-event time, against the L2 -> SM read bandwidth measured in this run",
+        "peak_source": "grgx_measure_l2_bandwidth in this run (an L2-resident buffer read by every SM); the "
+                       "ncu cross-check is in profiles/l2_ceiling_small.md",
+        "sweep_ms_per_step": sweep_s_step * 1e3,
+        "hbm": {"achieved": None if traffic is None else traffic / sweep_s_step / 1e9, "peak": hbm_peak,
+                "unit": "GB/s", "frac": None if traffic is None else traffic / sweep_s_step / 1e9 / hbm_peak,
+                "peak_source": hbm_src, "what": "measured DRAM bytes (scaled ncu capture) / sweep time"},
+        "edge_id_stream": id_stream,
+        "gather_model_GBps": abytes / sweep_s_step / 1e9,
+        "gather_model_note": "the survey's algorithmic bytes (ids, offsets, one row per edge, one row per node, "
+                             "I/O) / sweep time: exceeds the HBM peak because L2 serves the row gathers; not a "
+                             "fraction of any peak",
+        "compulsory_GBps": compulsory / sweep_s_step / 1e9,
+    }
 
     # end to end: host buffers through the C-ABI (copies inside the timed region)
     barrier()
     h2d = sum(V.nbytes for V in host_inputs)
     d2h = sum(K * (stats["mutations"] if d == UP else stats["samples"]) * dt.itemsize for dt, K, d in combos)
     e2e_value = e2e_mean = e2e_sync = None
-    e2e_steps = 0
-    if not args.no_e2e:
+    e2e_steps, e2e_times = 0, []
+    if not args.no_e2e and world == 1:
         # inputs in pinned host memory (host_empty); every call copies its input in and its
         # result back inside the timed region
         pinned_inputs = []
@@ -641,27 +860,27 @@ def main():
         e2e_times = timed_steps(step_async)
         sync_times = timed_steps(lambda inputs: step(inputs, None))
         # median step: one host-side stall (page reclaim, another process) does not set the figure
-        e2e_value = units_per_step * world / statistics.median(e2e_times)
-        e2e_mean = units_per_step * world * e2e_steps / sum(e2e_times)
-        e2e_sync = {"value": units_per_step * world / statistics.median(sync_times),
+        e2e_value = units_per_step / statistics.median(e2e_times)
+        e2e_mean = units_per_step * e2e_steps / sum(e2e_times)
+        e2e_sync = {"value": units_per_step / statistics.median(sync_times),
                     "step_ms": [round(x * 1e3, 1) for x in sync_times],
                     "api": "grgl_gb300.matmul (one synchronous call at a time, as pygrgl.matmul)"}
         del pinned_inputs
 
     cold = None
-    if rank == 0 and not args.no_load:
+    if rank == 0 and world == 1 and not args.no_load:
         cold = cold_start(gx, torch, g)
 
     batched = serve = large = None
-    if rank == 0 and not args.no_serve:
+    if rank == 0 and world == 1 and not args.no_serve:
         rng2 = np.random.default_rng(11)
         nb = args.batch_requests
-        batched = [batched_vs_plain(gx, torch, g, stats["edges"], rng2, nb, 128,
+        batched = [batched_vs_plain(gx, torch, g, E, rng2, nb, 128,
                                     "K~U{1..128}, UP/DOWN 50/50, float32 compensated, half N(0,1) and half "
                                     "standardized inputs", std_every=2, err_sample=8),
-                   batched_vs_plain(gx, torch, g, stats["edges"], rng2, nb, 8,
+                   batched_vs_plain(gx, torch, g, E, rng2, nb, 8,
                                     "K~U{1..8}, UP/DOWN 50/50, float32 compensated, N(0,1) inputs"),
-                   batched_vs_plain(gx, torch, g, stats["edges"], rng2, nb, 1,
+                   batched_vs_plain(gx, torch, g, E, rng2, nb, 1,
                                     "K=1 (single-vector requests, the dot_product pattern), UP/DOWN 50/50, float32 "
                                     "compensated, N(0,1) inputs")]
         g2 = gx.window_tree_grg(max(2, args.samples // 4), max(1, args.mutations * 3 // 10), seed=args.seed + 1)
@@ -673,44 +892,51 @@ def main():
                  "runs": [served(gx, [g, g2], float(r), args.serve_seconds, args.serve_requests, rng2)
                           for r in args.serve_rates.split(",")]}
         del g2
-    if rank == 0 and not args.no_large:
-        large = large_graph(gx, torch, args, peak)
+    if rank == 0 and world == 1 and not args.no_large:
+        large = large_graph(gx, torch, args, l2_peak)
 
-    cpu = None
-    if rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(args, combos, args.cpu_seconds)
+    cpu = parity = None
+    if rank == 0 and world == 1 and not (args.no_cpu_baseline and args.no_parity):
+        import oracle
+
+        og = oracle_graph(g)
+        smp = CpuSampler(og, combos, host_inputs, oracle.host_threads())
+        del og
+        if not args.no_parity:
+            parity = parity_vs_oracle(gx, torch, g, None, [(np.int32, 1, UP), (np.int32, 1, DOWN), (np.int32, 8, UP),
+                                                           (np.int32, 8, DOWN), (np.float64, 8, UP),
+                                                           (np.float64, 8, DOWN), (np.float32, 8, UP),
+                                                           (np.float32, 8, DOWN)], seed=13, shards=smp.sh)
+            parity["graph"] = "the benchmark graph itself"
+        if not args.no_cpu_baseline:
+            cpu = cpu_baseline(args, combos, smp)
+        del smp
 
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "int32,float32,float64", "data": "synthetic (seeded window-tree GRG)",
-            "config": {"workload": workload_name(args, combos),
-                       "graph": stats, "l2": "inputs larger than L2 (edge CSR streamed every traversal)",
-                       "parallelism": "replicas" if world > 1 else "single GPU"},
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": traffic,
-                         "traffic_unit": "DRAM bytes per step, summed over the step's sweep launches (ncu, "
-                                         "profiles/sweep_traffic.json)",
-                         "l2_resident": True if traffic is None else traffic < 0.5 * abytes / args.steps,
-                         "dram_frac": None if traffic is None else traffic / (sweep_ms / args.steps / 1e3) / 1e9 / peak,
-                         "compulsory_frac": compulsory / (sweep_ms / 1000.0) / 1e9 / peak,
-                         "kernel": "grgx::sweep_kernel", "sweep_ms_per_step": sweep_ms / args.steps,
-                         "l2": {"achieved": gathered / (sweep_ms / 1e3) / 1e9, "peak": l2_peak, "unit": "GB/s",
-                                "frac": gathered / (sweep_ms / 1e3) / 1e9 / l2_peak,
-                                "what": "edge ids + one gathered row per edge vs the measured L2->SM read "
-                                        "bandwidth (grgx_measure_l2_bandwidth)"},
-                         "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback 6800"},
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "strong" if world > 1 else "weak",
+            "vs_baseline": None, "dtype": "int32,float32,float64",
+            "float64_accumulation": "scaled float pairs (hi + lo float32 words, ~48-bit significand; error <= "
+                                    "4.5e-13 x sum |terms| per run), native FP64 when a row's range needs it",
+            "data": "synthetic (seeded window-tree GRG)",
+            "config": workload_config(args, combos, stats),
+            "parallelism": (f"{world} GPUs, one window-aligned mutation range each: DOWN all-reduce, UP all-gather "
+                            "(NCCL)") if world > 1 else "single GPU",
+            "graph_levels": levels, "device_bytes": device_bytes,
+            "roofline": roofline,
             "clocks": clk,
             "gpu_launches": launches,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "steps": None if args.no_e2e else e2e_steps, "statistic": "median step",
-                    "mean_value": None if args.no_e2e else e2e_mean,
-                    "step_ms": None if args.no_e2e else [round(x * 1e3, 1) for x in e2e_times],
+                    "steps": None if e2e_value is None else e2e_steps, "statistic": "median step",
+                    "mean_value": e2e_mean,
+                    "step_ms": [round(x * 1e3, 1) for x in e2e_times] if e2e_times else None,
                     "api": "grgl_gb300.matmul_async on numpy inputs in pinned memory (C ABI grgx_matmul, host "
                            f"pointers, GRGX_FLAG_ASYNC), calls round-robin over {args.e2e_streams} CUDA streams",
                     "one_call_at_a_time": e2e_sync},
             "cpu_baseline": cpu,
+            "parity_full_size": parity,
             "batched_vs_plain": batched,
             "served": serve,
             "large_graph": large,
