@@ -54,6 +54,8 @@ def parse_args():
     ap.add_argument("--no-serve", action="store_true", help="skip the batched and served measurements")
     ap.add_argument("--batch-requests", type=int, default=256, help="requests in the batched measurement")
     ap.add_argument("--serve-rates", default="50,200,500,1000,2000", help="Poisson arrival rates (requests/s)")
+    ap.add_argument("--narrow-rates", default="10,100,1000",
+                    help="Poisson arrival rates (requests/s) of the narrow (K <= 8) served mix")
     ap.add_argument("--serve-seconds", type=float, default=4.0, help="longest arrival window of a served run")
     ap.add_argument("--serve-requests", type=int, default=96, help="most arrivals in a served run")
     ap.add_argument("--no-large", action="store_true", help="skip the large-graph measurement")
@@ -280,10 +282,12 @@ def batched_vs_plain(gx, torch, g, E, rng, n_req, kmax, label, std_every=0, err_
     return res
 
 
-def served(gx, graphs, rate, seconds, max_requests, rng):
-    """Poisson arrivals over resident graphs (K log-uniform in [1, 256], UP/DOWN and int32/float32
+def served(gx, graphs, rate, seconds, max_requests, rng, kmax=256):
+    """Poisson arrivals over resident graphs (K log-uniform in [1, kmax], UP/DOWN and int32/float32
     mixed), served by the continuous-batching server; against the same requests one per call.
-    The arrival window is `seconds`, cut short after `max_requests` arrivals."""
+    The arrival window is `seconds`, cut short after `max_requests` arrivals.  Each request's own
+    time alone (one synchronous call, host buffers as in the served path) is measured too, so a
+    rate below the server's capacity shows latency = service time, not queueing."""
     import threading
 
     sizes = [(g.num_samples, g.num_mutations, g.num_edges) for g in graphs]
@@ -299,7 +303,7 @@ def served(gx, graphs, rate, seconds, max_requests, rng):
         if t > seconds:
             break
         gi = 0 if (len(graphs) == 1 or rng.random() < 0.7) else 1
-        K = int(np.exp(rng.uniform(0.0, np.log(256.0))))
+        K = int(np.exp(rng.uniform(0.0, np.log(float(kmax)))))
         d = UP if rng.random() < 0.5 else DOWN
         dt = "int32" if rng.random() < 0.5 else "float32"
         arrivals.append((t, gi, d, pools[(gi, d, dt)][:K]))
@@ -336,8 +340,11 @@ def served(gx, graphs, rate, seconds, max_requests, rng):
         t_served = time.perf_counter() - t0
     t0 = time.perf_counter()
     alone = {}
+    alone_ms = []
     for i, (_, gi, d, V) in enumerate(arrivals):
+        t1 = time.perf_counter()
         r = gx.matmul(graphs[gi], V, d)
+        alone_ms.append(1e3 * (time.perf_counter() - t1))
         if i in kept:
             alone[i] = r
     t_plain = time.perf_counter() - t0
@@ -352,9 +359,11 @@ def served(gx, graphs, rate, seconds, max_requests, rng):
             scale = max(float(np.max(np.abs(a))), 1e-30)
             f32_diff = max(f32_diff, float(np.max(np.abs(a.astype(np.float64) - b))) / scale)
     lat_ms = np.array(lat) * 1e3
-    return {"arrival_rate_per_s": rate, "requests": len(arrivals),
+    return {"arrival_rate_per_s": rate, "requests": len(arrivals), "k_max": kmax,
             "arrival_window_s": arrivals[-1][0] if arrivals else 0.0,
             "p50_ms": float(np.percentile(lat_ms, 50)), "p99_ms": float(np.percentile(lat_ms, 99)),
+            "alone_p50_ms": float(np.percentile(alone_ms, 50)),
+            "p50_over_alone_p50": float(np.percentile(lat_ms, 50) / max(np.percentile(alone_ms, 50), 1e-9)),
             "served_edgeK_per_s": units / t_served, "plain_sequential_edgeK_per_s": units / t_plain,
             "mean_batch_requests": float(np.mean(batches)),
             "mix_vs_alone": {"checked": len(alone), "int32_bit_exact": int_exact,
@@ -890,7 +899,10 @@ def main():
                         "70% of requests on the first graph",
                  "plain": "the same requests one per call, sequentially",
                  "runs": [served(gx, [g, g2], float(r), args.serve_seconds, args.serve_requests, rng2)
-                          for r in args.serve_rates.split(",")]}
+                          for r in args.serve_rates.split(",")],
+                 "narrow_mix": "K log-uniform in [1, 8], otherwise as above",
+                 "narrow_runs": [served(gx, [g, g2], float(r), args.serve_seconds, args.serve_requests, rng2,
+                                        kmax=8) for r in args.narrow_rates.split(",")]}
         del g2
     if rank == 0 and world == 1 and not args.no_large:
         large = large_graph(gx, torch, args, l2_peak)

@@ -50,6 +50,34 @@ size_t elem_bytes(int dtype) {
     }
 }
 
+// Streams a batch spreads its traversals over (per host thread, created on first use): a
+// batch's stacks -- UP and DOWN ones, different dtypes -- run side by side instead of one after
+// the other.
+constexpr int kBatchStreams = 3;
+struct BatchStreams {
+    cudaStream_t s[kBatchStreams] = {};
+    int device = -1;
+    ~BatchStreams() {
+        for (cudaStream_t x : s)
+            if (x) cudaStreamDestroy(x);
+    }
+};
+thread_local BatchStreams t_streams;
+
+cudaStream_t* batch_streams() {
+    int device = 0;
+    BATCH_CUDA(cudaGetDevice(&device));
+    if (t_streams.device != device) {
+        for (cudaStream_t& x : t_streams.s) {
+            if (x) cudaStreamDestroy(x);
+            x = nullptr;
+        }
+        for (cudaStream_t& x : t_streams.s) BATCH_CUDA(cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking));
+        t_streams.device = device;
+    }
+    return t_streams.s;
+}
+
 }  // namespace
 
 // Default stacking width: 512 four-byte or 256 eight-byte columns.  A traversal's cost per
@@ -86,77 +114,112 @@ void matmul_batch_impl(grgx_graph* g, const grgx_request* reqs, uint64_t n, uint
     }
     const uint32_t passFlags = (flags & (GRGX_FLAG_F32_PLAIN | GRGX_FLAG_F64_NATIVE)) | GRGX_FLAG_DEVICE_POINTERS |
                                GRGX_FLAG_OVERWRITE;
+    // The stacks: per group, requests in order while the stacked rows fit `width` (a wider
+    // request runs alone).
+    struct Stack {
+        int direction, dtype, byIndiv;
+        std::vector<uint64_t> req;
+        uint64_t rows;
+    };
+    std::vector<Stack> stacks;
     for (auto& kv : groups) {
         const int direction = std::get<0>(kv.first), dtype = std::get<1>(kv.first), byIndiv = std::get<2>(kv.first);
-        const uint64_t sampleCols = byIndiv ? hg.num_samples / hg.ploidy : hg.num_samples;
-        const uint64_t cols = (direction == GRGX_DIRECTION_UP) ? sampleCols : hg.num_mutations;
-        const uint64_t outCols = (direction == GRGX_DIRECTION_UP) ? hg.num_mutations : sampleCols;
-        const size_t es = elem_bytes(dtype);
         const uint64_t width = maxCols ? maxCols : default_batch_cols(dtype);
         const std::vector<uint64_t>& idx = kv.second;
         size_t i = 0;
         while (i < idx.size()) {
-            // greedy: stack requests in order while the stacked rows fit `width` (a wider request
-            // runs alone)
-            uint64_t rowsTotal = reqs[idx[i]].rows;
+            Stack st{direction, dtype, byIndiv, {idx[i]}, reqs[idx[i]].rows};
             size_t j = i + 1;
-            while (j < idx.size() && rowsTotal + reqs[idx[j]].rows <= width) rowsTotal += reqs[idx[j++]].rows;
-            if (j == i + 1) {
-                const grgx_request& r = reqs[idx[i]];
-                if (r.options & GRGX_REQUEST_STANDARDIZED)
-                    matmul_standardized_impl(g, dtype, r.input, cols, r.rows, direction, r.output, r.rows * outCols,
-                                             flags & ~GRGX_FLAG_SYNC, stream);
-                else
-                    matmul_impl(g, dtype, r.input, cols, r.rows, direction, r.output, r.rows * outCols, 0, byIndiv,
-                                nullptr, GRGX_INIT_ZERO, nullptr, (flags & ~GRGX_FLAG_SYNC) | GRGX_FLAG_OVERWRITE,
-                                stream);
-                i = j;
-                continue;
+            while (j < idx.size() && st.rows + reqs[idx[j]].rows <= width) {
+                st.rows += reqs[idx[j]].rows;
+                st.req.push_back(idx[j++]);
             }
-            bool anyStd = false;
-            for (size_t k = i; k < j; k++) anyStd |= (reqs[idx[k]].options & GRGX_REQUEST_STANDARDIZED) != 0;
-            DevicePlan* dp = anyStd ? standardized_plan(g, s) : nullptr;
-            double* red = nullptr;
-            if (anyStd) BATCH_CUDA(pool_malloc(reinterpret_cast<void**>(&red), rowsTotal * sizeof(double), s));
-            void* in = nullptr;
-            void* out = nullptr;
-            BATCH_CUDA(pool_malloc(&in, rowsTotal * cols * es, s));
-            BATCH_CUDA(pool_malloc(&out, rowsTotal * outCols * es, s));
-            uint64_t row = 0;
-            for (size_t k = i; k < j; k++) {
-                const grgx_request& r = reqs[idx[k]];
-                char* rowsIn = static_cast<char*>(in) + row * cols * es;
-                BATCH_CUDA(cudaMemcpyAsync(rowsIn, r.input, r.rows * cols * es,
-                                           dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
-                if ((r.options & GRGX_REQUEST_STANDARDIZED) && direction == GRGX_DIRECTION_DOWN)
-                    standardized_prepare_down(dtype, dp, rowsIn, static_cast<long long>(r.rows),
-                                              static_cast<long long>(cols), red + row, s);
-                row += r.rows;
-            }
-            matmul_impl(g, dtype, in, cols, rowsTotal, direction, out, rowsTotal * outCols, 0, byIndiv, nullptr,
-                        GRGX_INIT_ZERO, nullptr, passFlags, stream);
-            row = 0;
-            for (size_t k = i; k < j; k++) {
-                const grgx_request& r = reqs[idx[k]];
-                char* rowsOut = static_cast<char*>(out) + row * outCols * es;
-                if (r.options & GRGX_REQUEST_STANDARDIZED) {
-                    if (direction == GRGX_DIRECTION_DOWN)
-                        standardized_finish_down(dtype, rowsOut, red + row, static_cast<long long>(r.rows),
-                                                 static_cast<long long>(outCols), s);
-                    else
-                        standardized_finish_up(dtype, dp, static_cast<char*>(in) + row * cols * es,
-                                               static_cast<long long>(r.rows), static_cast<long long>(cols), rowsOut,
-                                               static_cast<long long>(outCols), red + row, s);
-                }
-                BATCH_CUDA(cudaMemcpyAsync(r.output, rowsOut,
-                                           r.rows * outCols * es,
-                                           dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
-                row += r.rows;
-            }
-            BATCH_CUDA(cudaFreeAsync(in, s));
-            BATCH_CUDA(cudaFreeAsync(out, s));
-            if (red) BATCH_CUDA(cudaFreeAsync(red, s));
+            stacks.push_back(std::move(st));
             i = j;
+        }
+    }
+    // Several stacks: fork them over the batch streams (round robin, after the work already queued
+    // on the caller's stream) and join them back onto it at the end.
+    const int nstreams = static_cast<int>(std::min<size_t>(kBatchStreams, stacks.size()));
+    cudaStream_t* bs = nstreams > 1 ? batch_streams() : nullptr;
+    cudaEvent_t fork = nullptr;
+    if (nstreams > 1) {
+        BATCH_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+        BATCH_CUDA(cudaEventRecord(fork, s));
+        for (int k = 0; k < nstreams; k++) BATCH_CUDA(cudaStreamWaitEvent(bs[k], fork, 0));
+        BATCH_CUDA(cudaEventDestroy(fork));
+    }
+    for (size_t si = 0; si < stacks.size(); si++) {
+        const Stack& st = stacks[si];
+        cudaStream_t ss = nstreams > 1 ? bs[si % nstreams] : s;
+        const int direction = st.direction, dtype = st.dtype, byIndiv = st.byIndiv;
+        const uint64_t sampleCols = byIndiv ? hg.num_samples / hg.ploidy : hg.num_samples;
+        const uint64_t cols = (direction == GRGX_DIRECTION_UP) ? sampleCols : hg.num_mutations;
+        const uint64_t outCols = (direction == GRGX_DIRECTION_UP) ? hg.num_mutations : sampleCols;
+        const size_t es = elem_bytes(dtype);
+        if (st.req.size() == 1) {
+            const grgx_request& r = reqs[st.req[0]];
+            // host buffers on a batch stream are queued asynchronously; the join below orders them
+            const uint32_t f = (flags & ~GRGX_FLAG_SYNC) | (nstreams > 1 && !dev ? GRGX_FLAG_ASYNC : 0u);
+            if (r.options & GRGX_REQUEST_STANDARDIZED)
+                matmul_standardized_impl(g, dtype, r.input, cols, r.rows, direction, r.output, r.rows * outCols, f,
+                                         ss);
+            else
+                matmul_impl(g, dtype, r.input, cols, r.rows, direction, r.output, r.rows * outCols, 0, byIndiv,
+                            nullptr, GRGX_INIT_ZERO, nullptr, f | GRGX_FLAG_OVERWRITE, ss);
+            continue;
+        }
+        const uint64_t rowsTotal = st.rows;
+        bool anyStd = false;
+        for (uint64_t k : st.req) anyStd |= (reqs[k].options & GRGX_REQUEST_STANDARDIZED) != 0;
+        DevicePlan* dp = anyStd ? standardized_plan(g, ss) : nullptr;
+        double* red = nullptr;
+        if (anyStd) BATCH_CUDA(pool_malloc(reinterpret_cast<void**>(&red), rowsTotal * sizeof(double), ss));
+        void* in = nullptr;
+        void* out = nullptr;
+        BATCH_CUDA(pool_malloc(&in, rowsTotal * cols * es, ss));
+        BATCH_CUDA(pool_malloc(&out, rowsTotal * outCols * es, ss));
+        uint64_t row = 0;
+        for (uint64_t k : st.req) {
+            const grgx_request& r = reqs[k];
+            char* rowsIn = static_cast<char*>(in) + row * cols * es;
+            BATCH_CUDA(cudaMemcpyAsync(rowsIn, r.input, r.rows * cols * es,
+                                       dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, ss));
+            if ((r.options & GRGX_REQUEST_STANDARDIZED) && direction == GRGX_DIRECTION_DOWN)
+                standardized_prepare_down(dtype, dp, rowsIn, static_cast<long long>(r.rows),
+                                          static_cast<long long>(cols), red + row, ss);
+            row += r.rows;
+        }
+        matmul_impl(g, dtype, in, cols, rowsTotal, direction, out, rowsTotal * outCols, 0, byIndiv, nullptr,
+                    GRGX_INIT_ZERO, nullptr, passFlags, ss);
+        row = 0;
+        for (uint64_t k : st.req) {
+            const grgx_request& r = reqs[k];
+            char* rowsOut = static_cast<char*>(out) + row * outCols * es;
+            if (r.options & GRGX_REQUEST_STANDARDIZED) {
+                if (direction == GRGX_DIRECTION_DOWN)
+                    standardized_finish_down(dtype, rowsOut, red + row, static_cast<long long>(r.rows),
+                                             static_cast<long long>(outCols), ss);
+                else
+                    standardized_finish_up(dtype, dp, static_cast<char*>(in) + row * cols * es,
+                                           static_cast<long long>(r.rows), static_cast<long long>(cols), rowsOut,
+                                           static_cast<long long>(outCols), red + row, ss);
+            }
+            BATCH_CUDA(cudaMemcpyAsync(r.output, rowsOut, r.rows * outCols * es,
+                                       dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, ss));
+            row += r.rows;
+        }
+        BATCH_CUDA(cudaFreeAsync(in, ss));
+        BATCH_CUDA(cudaFreeAsync(out, ss));
+        if (red) BATCH_CUDA(cudaFreeAsync(red, ss));
+    }
+    if (nstreams > 1) {
+        for (int k = 0; k < nstreams; k++) {
+            cudaEvent_t join = nullptr;
+            BATCH_CUDA(cudaEventCreateWithFlags(&join, cudaEventDisableTiming));
+            BATCH_CUDA(cudaEventRecord(join, bs[k]));
+            BATCH_CUDA(cudaStreamWaitEvent(s, join, 0));
+            BATCH_CUDA(cudaEventDestroy(join));
         }
     }
     if (!dev || (flags & GRGX_FLAG_SYNC)) BATCH_CUDA(cudaStreamSynchronize(s));
