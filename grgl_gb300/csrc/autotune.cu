@@ -147,21 +147,31 @@ std::string autotune_impl(grgx_graph* g, int dtype, uint64_t rows, int direction
     const bool down = (direction == GRGX_DIRECTION_DOWN);
     // the CSRs a call of this shape sweeps; for UP both forms when the split form is possible,
     // so the faster one is recorded for this graph
+    // (for DOWN too: the height-0 level in parent blocks, the levels above it as usual)
     struct Pass {
         const DevCSR* c;
         int mode;
         const char* name;
+        long long stateBase;
+        bool skipLast;  // the CSR's last level is left to the next pass
     };
     std::vector<std::vector<Pass>> forms;
-    const bool trySplit = !down && up_split_possible(dp);
+    const long long h0 = static_cast<long long>(dp->level_begin.size() > 1 ? dp->level_begin[1] : 0);
     if (down) {
-        forms.push_back({{&dp->down, 0, "level"}});
+        forms.push_back({{&dp->down, 0, "level", 0, false}});
+        if (down_split_possible(dp)) {
+            ensure_down_split(g, dp);
+            if (dp->down0b.n_rows > 0)
+                forms.push_back({{&dp->down, 0, "split: level", 0, true},
+                                 {&dp->down0b, 1, "split: height-0 parent block", 0, false}});
+        }
     } else {
-        forms.push_back({{&dp->up, 0, "level"}});
-        if (trySplit) {
+        forms.push_back({{&dp->up, 0, "level", 0, false}});
+        if (up_split_possible(dp)) {
             ensure_up_split(g, dp);
             if (dp->up0b.n_rows > 0)
-                forms.push_back({{&dp->up0b, 1, "split: height-0 block"}, {&dp->up_int, 2, "split: level"}});
+                forms.push_back({{&dp->up0b, 1, "split: height-0 block", dp->split_src, false},
+                                 {&dp->up_int, 2, "split: level", dp->split_src, false}});
         }
     }
     long long maxPieces = 0, maxHeavy = 0;
@@ -194,7 +204,8 @@ std::string autotune_impl(grgx_graph* g, int dtype, uint64_t rows, int direction
         GRGX_CUDA(cudaMemsetAsync(vals, 0, valBytes, s));
         GRGX_CUDA(cudaMalloc(&partials, std::max<size_t>(static_cast<size_t>(maxPieces) * L.stride * L.asize, 16)));
         if (needState) {
-            const size_t stateBytes = (n - static_cast<size_t>(dp->split_src)) * L.stride * std::max(L.asize, 8);
+            const size_t stateRows = down ? static_cast<size_t>(h0) : n - static_cast<size_t>(dp->split_src);
+            const size_t stateBytes = stateRows * L.stride * std::max(L.asize, 8);
             GRGX_CUDA(cudaMalloc(&state, std::max<size_t>(stateBytes, 16)));
             GRGX_CUDA(cudaMemsetAsync(state, 0, stateBytes, s));
         }
@@ -207,13 +218,14 @@ std::string autotune_impl(grgx_graph* g, int dtype, uint64_t rows, int direction
         const int rmw = down ? 1 : 0;
         const DevCSR* cur = nullptr;
         int curMode = 0;
+        long long curBase = 0;
         auto time_shape = [&](size_t lvl, const LevelShape& sh) {
             float best = 1e30f;
             for (int rep_i = 0; rep_i < 3; rep_i++) {
                 GRGX_CUDA(cudaMemsetAsync(counters, 0, counterBytes, s));
                 GRGX_CUDA(cudaEventRecord(e0, s));
-                launch_level(L, *cur, lvl, vals, vals, rmw, partials, tickets, work, s, nullptr, 0, &sh, maxT,
-                             curMode ? state : nullptr, dp->split_src, curMode ? curMode : 1);
+                launch_level(L, *cur, lvl, vals, vals, curMode == 1 ? 0 : rmw, partials, tickets, work, s, nullptr, 0,
+                             &sh, maxT, curMode ? state : nullptr, curBase, curMode ? curMode : 1);
                 GRGX_CUDA(cudaEventRecord(e1, s));
                 GRGX_CUDA(cudaEventSynchronize(e1));
                 GRGX_CUDA(cudaGetLastError());
@@ -232,8 +244,9 @@ std::string autotune_impl(grgx_graph* g, int dtype, uint64_t rows, int direction
             for (const Pass& ps : form) {
                 cur = ps.c;
                 curMode = ps.mode;
+                curBase = ps.stateBase;
                 const DevCSR& c = *ps.c;
-                for (size_t lvl = 0; lvl < c.lb.size(); lvl++) {
+                for (size_t lvl = 0; lvl + (ps.skipLast ? 1 : 0) < c.lb.size(); lvl++) {
                     if (c.le[lvl] <= c.lb[lvl]) continue;
                     const LevelShape def = default_shape(L);
                     const float tDef = time_shape(lvl, def);
@@ -278,16 +291,22 @@ std::string autotune_impl(grgx_graph* g, int dtype, uint64_t rows, int direction
                 }
             }
             char tail[160];
+            const bool splitForm = (&form != &forms[0]);
             std::snprintf(tail, sizeof(tail), "%s %.4f ms tuned, %.4f ms default\n",
-                          forms.size() > 1 ? (form[0].mode ? "split sweep" : "unsplit sweep") : "sweep", totBest,
+                          forms.size() > 1 ? (splitForm ? "split sweep" : "unsplit sweep") : "sweep", totBest,
                           totDefault);
             rep << tail;
             formBest.push_back(totBest);
         }
         if (forms.size() > 1) {
             const bool split = formBest[1] < 0.98 * formBest[0];
-            set_up_split_choice(g, dp, L, split);
-            rep << (split ? "UP runs in split form for this shape\n" : "UP runs unsplit for this shape\n");
+            if (down) {
+                set_down_split_choice(g, dp, L, split);
+                rep << (split ? "DOWN runs in split form for this shape\n" : "DOWN runs unsplit for this shape\n");
+            } else {
+                set_up_split_choice(g, dp, L, split);
+                rep << (split ? "UP runs in split form for this shape\n" : "UP runs unsplit for this shape\n");
+            }
         }
     } catch (...) {
         release();

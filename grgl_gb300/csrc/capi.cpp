@@ -27,6 +27,8 @@ void matmul_standardized_impl(grgx_graph* g, int dtype, const void* input, uint6
 void matmul_gram_impl(grgx_graph* g, int dtype, const void* input, uint64_t in_cols, uint64_t rows, int first,
                       void* output, uint64_t output_size, int standardized, uint32_t flags, void* stream);
 void set_up_split(long long block, unsigned long long thresholdBytes);
+void set_down_split_mode(int mode);
+void set_staged(bool on);
 void* host_alloc(uint64_t bytes);
 void host_free(void* b);
 std::string autotune_impl(grgx_graph* g, int dtype, uint64_t rows, int direction, uint32_t flags);
@@ -440,6 +442,13 @@ extern "C" grgx_status grgx_debug_host_plan(grgx_graph* g, const char* name, con
 // built from now on (0 keeps it) and the height-0 row bytes above which UP runs in split form.
 extern "C" void grgx_debug_up_split(long long block, unsigned long long threshold_bytes) {
     grgx::set_up_split(block, threshold_bytes);
+}
+
+// Test hook (not part of the public header): DOWN split form by rule (0), always (1) or never
+// (2); single-column split passes staged in shared memory (1) or gathered from global memory (0).
+extern "C" void grgx_debug_split_forms(int down_mode, int staged) {
+    grgx::set_down_split_mode(down_mode);
+    grgx::set_staged(staged != 0);
 }
 
 grgx_status grgx_collect_timings(grgx_timing* out, uint64_t capacity, uint64_t* count) {

@@ -22,7 +22,10 @@ namespace grgx {
     } while (0)
 
 struct DevCSR {
-    uint32_t* adj = nullptr;
+    uint32_t* adj = nullptr;  // 32-bit ids, or 16-bit block-relative ids when id16
+    bool id16 = false;
+    // id16: per level (= split block), the block's first source id and its number of source ids
+    std::vector<long long> level_base, level_src_rows;
     int* rows = nullptr;
     ChunkDev* chunks = nullptr;
     HeavyDev* heavy = nullptr;
@@ -48,6 +51,19 @@ struct DevicePlan {
     long long split_block = 0, split_src = 0;  // split_src = height-0 ids = first UP row's node id
     bool split_built = false;
     std::map<std::pair<int, long long>, bool> split_choice;  // (storage kind, stride) -> measured choice
+    // DOWN in split form (empty when the parents of height-0 rows make fewer than two blocks):
+    //   down0b  the edges of the height-0 DOWN rows, cut by blocks of `split_block` parent ids
+    //           starting at split_src (parents all have height >= 1); level j = block j, rows =
+    //           every height-0 row with parents in the block; 16-bit block-relative ids
+    //   fin_down the height-0 DOWN rows, finished from their state after the block passes
+    // Built on the first call that runs DOWN in split form (use_down_split).
+    DevCSR down0b;
+    int* fin_down = nullptr;
+    long long n_fin_down = 0;
+    bool down_split_built = false;
+    std::map<std::pair<int, long long>, bool> down_split_choice;
+    std::vector<int64_t> down_off;       // DOWN row offsets (host copy)
+    long long down_h0_row = 0;           // first DOWN row of height 0
     std::vector<int64_t> up_off;         // UP row offsets (host copy)
     std::vector<uint64_t> level_begin;   // node-id range of each height
     uint32_t* mut_new = nullptr;
@@ -118,6 +134,22 @@ bool use_up_split(grgx_graph* g, DevicePlan* dp, const Layout& L);
 bool up_split_possible(const DevicePlan* dp);
 void ensure_up_split(grgx_graph* g, DevicePlan* dp);
 void set_up_split_choice(grgx_graph* g, DevicePlan* dp, const Layout& L, bool split);
+// The same for DOWN: the height-0 level in parent blocks.  Without a measured choice a call runs
+// DOWN in split form when its block passes run staged (staged_layout); UP likewise, or when the
+// height-0 rows exceed the threshold.
+bool use_down_split(grgx_graph* g, DevicePlan* dp, const Layout& L);
+bool down_split_possible(const DevicePlan* dp);
+void ensure_down_split(grgx_graph* g, DevicePlan* dp);
+void set_down_split_choice(grgx_graph* g, DevicePlan* dp, const Layout& L, bool split);
+// Whether single-column 4-byte split passes stage their block's source values in shared memory
+// (sweep_kernel_staged); on by default, switchable for tests.
+bool staged_enabled();
+void set_staged(bool on);
+// Whether split block passes of layout L run staged: a single 4-byte column (K = 1 for the
+// 4-byte dtypes, bool up to 32 columns), staging on.
+bool staged_layout(const Layout& L);
+// DOWN split form: 0 chosen as above, 1 always (where possible), 2 never (tests).
+void set_down_split_mode(int mode);
 
 // Resolves (once per device, with `device` current) the address of grgx_matmul_noalloc's
 // static scratch, which loads its module and so reserves the array on the device.

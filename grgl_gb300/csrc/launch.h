@@ -32,6 +32,13 @@ void launch_sweep_f32(const SweepParams<float>& p, int vw, int g, int variant, d
 void launch_sweep_f64s(const SweepParams<DF>& p, int vw, int g, int variant, dim3 grid,
                       int sms, cudaStream_t s);
 
+// Staged single-column sweeps of one split block (sweep_kernel_staged; p.src = the block's first
+// source value, p.src_rows <= kStagedRows values), 4-byte storage kinds.
+void launch_sweep_staged_u32(const SweepParams<uint32_t>& p, dim3 grid, cudaStream_t s);
+void launch_sweep_staged_xor(const SweepParams<uint32_t>& p, dim3 grid, cudaStream_t s);
+void launch_sweep_staged_f32c(const SweepParams<float>& p, dim3 grid, cudaStream_t s);
+void launch_sweep_staged_f32(const SweepParams<float>& p, dim3 grid, cudaStream_t s);
+
 // Column-map modes of the transposing loads/stores.
 enum MapMode { MAP_IDENT = 0, MAP_DIV = 1, MAP_TABLE = 2, MAP_FOLD = 3 };
 

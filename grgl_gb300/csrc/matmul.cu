@@ -203,6 +203,9 @@ SweepParams<S> make_params(const DevCSR& c, long long cb, long long ce, const vo
     p.state = nullptr;
     p.state_base = 0;
     p.state_mode = 0;
+    p.id16 = 0;
+    p.id_base = 0;
+    p.src_rows = 0;
     return p;
 }
 
@@ -230,6 +233,48 @@ int launch_level(const Layout& L, const DevCSR& c, size_t level, const void* src
         return p;
     };
     const int vw = L.vw, g = sh.g, v = sh.variant;
+    if (c.id16) {
+        // a split block: 16-bit ids relative to the block's first source id.  Single-column
+        // 4-byte rows stage the block's sources in shared memory (one 1024-thread block per SM).
+        const long long base = c.level_base[level], srows = c.level_src_rows[level];
+        const bool staged = staged_layout(L) && srows <= kStagedRows && sh.ntiles == 1;
+        if (staged) {
+            const dim3 sgrid(static_cast<unsigned>(std::min<long long>((ce - cb + 7) / 8, sms)), 1);
+            auto sp = [&](auto tag) {
+                using S = decltype(tag);
+                SweepParams<S> p = prm(tag);
+                p.id16 = 1;
+                p.id_base = 0;
+                p.src = static_cast<const S*>(src) + base;
+                p.src_rows = srows;
+                return p;
+            };
+            switch (L.kind) {
+            case Kind::U32: launch_sweep_staged_u32(sp(uint32_t{}), sgrid, s); break;
+            case Kind::XOR: launch_sweep_staged_xor(sp(uint32_t{}), sgrid, s); break;
+            case Kind::F32C: launch_sweep_staged_f32c(sp(float{}), sgrid, s); break;
+            case Kind::F32: launch_sweep_staged_f32(sp(float{}), sgrid, s); break;
+            default: break;
+            }
+            return 1;
+        }
+        auto ip = [&](auto tag) {
+            auto p = prm(tag);
+            p.id16 = 1;
+            p.id_base = base;
+            return p;
+        };
+        switch (L.kind) {
+        case Kind::U32: launch_sweep_u32(ip(uint32_t{}), vw, g, v, grid, sms, s); break;
+        case Kind::XOR: launch_sweep_xor(ip(uint32_t{}), vw, g, v, grid, sms, s); break;
+        case Kind::U64: launch_sweep_u64(ip(static_cast<unsigned long long>(0)), vw, g, v, grid, sms, s); break;
+        case Kind::F64: launch_sweep_f64(ip(double{}), vw, g, v, grid, sms, s); break;
+        case Kind::F32C: launch_sweep_f32c(ip(float{}), vw, g, v, grid, sms, s); break;
+        case Kind::F32: launch_sweep_f32(ip(float{}), vw, g, v, grid, sms, s); break;
+        case Kind::F64S: launch_sweep_f64s(ip(DF{}), vw, g, v, grid, sms, s); break;
+        }
+        return 1;
+    }
     switch (L.kind) {
     case Kind::U32: launch_sweep_u32(prm(uint32_t{}), vw, g, v, grid, sms, s); break;
     case Kind::XOR: launch_sweep_xor(prm(uint32_t{}), vw, g, v, grid, sms, s); break;
@@ -376,6 +421,9 @@ DevicePlan* ensure_device_plan_once(grgx_graph* g) {
     for (uint32_t x : hp.xtx_new)
         if (x != COAL_NOT_SET) d->xtx_max = std::max(d->xtx_max, static_cast<double>(x));
     d->up_off = hp.up.off;
+    d->down_off = hp.down.off;
+    if (!hp.down.level_chunk_begin.empty())
+        d->down_h0_row = hp.down.chunks[static_cast<size_t>(hp.down.level_chunk_begin.back())].r0;
     d->level_begin = hp.level_begin;
     g->dev = std::move(d);
     g->plan.reset();  // the device copy is authoritative; free the host copy
@@ -510,16 +558,24 @@ void matmul_direct(grgx_graph* g, int dtype, const void* input, uint64_t in_cols
         // UP in split form when the height-0 rows outgrow L2: their edges first, in blocked
         // passes, then the other edges level by level (up_split.cu)
         const bool split = !down && use_up_split(g, dp, L);
+        // DOWN in split form: the height-0 level in parent blocks (up_split.cu)
+        const bool dsplit = down && use_down_split(g, dp, L);
         long long pieces = down ? std::max(dp->down.n_pieces, std::max(dp->seed.n_pieces, dp->miss.n_pieces))
                                 : (split ? std::max(dp->up0b.n_pieces, dp->up_int.n_pieces) : dp->up.n_pieces);
+        if (dsplit) pieces = std::max(pieces, dp->down0b.n_pieces);
         void* partials = sc.get(static_cast<size_t>(pieces) * L.stride * L.asize);
-        const long long nh = down ? (dp->down.n_heavy + dp->seed.n_heavy + dp->miss.n_heavy)
+        const long long nh = down ? (dp->down.n_heavy + dp->seed.n_heavy + dp->miss.n_heavy +
+                                     (dsplit ? dp->down0b.n_heavy : 0))
                                   : (split ? dp->up0b.n_heavy + dp->up_int.n_heavy : dp->up.n_heavy);
-        const long long nslots = down ? (2 + static_cast<long long>(dp->down.lb.size()))
+        const long long nslots = down ? (2 + static_cast<long long>(dp->down.lb.size()) +
+                                         (dsplit ? static_cast<long long>(dp->down0b.lb.size()) : 0))
                                       : static_cast<long long>(split ? dp->up0b.lb.size() + dp->up_int.lb.size()
                                                                      : dp->up.lb.size());
-        const size_t stateBytes = split ? static_cast<size_t>(n - dp->split_src) * L.stride * std::max(L.asize, 8) : 0;
-        void* state = split ? sc.get(stateBytes) : nullptr;
+        const long long h0 = static_cast<long long>(dp->level_begin.size() > 1 ? dp->level_begin[1] : 0);
+        const size_t stateBytes = split    ? static_cast<size_t>(n - dp->split_src) * L.stride * std::max(L.asize, 8)
+                                  : dsplit ? static_cast<size_t>(h0) * L.stride * std::max(L.asize, 8)
+                                           : 0;
+        void* state = (split || dsplit) ? sc.get(stateBytes) : nullptr;
         // counters per launch and per heavy row: enough column tiles for any launch shape
         const int TS = max_tiles(L);
         const size_t counterBytes = static_cast<size_t>(nh + nslots) * TS * sizeof(unsigned);
@@ -624,8 +680,26 @@ void matmul_direct(grgx_graph* g, int dtype, const void* input, uint64_t in_cols
                 }
                 tk += dp->miss.n_heavy * TS;
                 if (timed && t_timing) GRGX_CUDA(cudaEventRecord(ev[1], s));
-                for (size_t lvl = 0; lvl < dp->down.lb.size(); lvl++)
+                const size_t nlv = dp->down.lb.size();
+                for (size_t lvl = 0; lvl < nlv; lvl++) {
+                    if (dsplit && lvl + 1 == nlv) break;  // the height-0 level runs in split form below
                     launches += level(dp->down, lvl, vals, 1, tk, work + (2 + lvl) * TS);
+                }
+                if (dsplit) {
+                    // parent-block passes merge each height-0 row's sums into its state; then the
+                    // rows are written from it, onto their seed / init values
+                    GRGX_CUDA(cudaMemsetAsync(state, 0, stateBytes, s));
+                    unsigned* tS = tk + dp->down.n_heavy * TS;
+                    unsigned* wS = work + (2 + nlv) * TS;
+                    for (size_t j = 0; j < dp->down0b.lb.size(); j++) {
+                        const LevelShape sh = level_shape(LL, dp->down0b, j);
+                        launches += launch_level(LL, dp->down0b, j, vals, vals, 0, partials, tS, wS + j * TS, s, g,
+                                                 gv, &sh, TS, state, 0, 1);
+                    }
+                    launch_state_finish(LL.kind, state, vals, dp->fin_down, dp->n_fin_down, 0, LL.stride, 1, s, g,
+                                        gv);
+                    launches++;
+                }
                 if (timed && t_timing) GRGX_CUDA(cudaEventRecord(ev[2], s));
                 if (emit_all) {
                     store_cols(n, MAP_TABLE, 1, dp->old2new, dOut, out_cols, add);

@@ -52,7 +52,26 @@ template <typename S> struct SweepParams {
     void* state;               // per-node Op::A carried between launches (UP split passes), or null
     long long state_base;      // node id of the first state row
     int state_mode;            // 1: merge each row sum into its state; 2: write state + row sum
+    // Edge-id format.  id16 = 0: 32-bit source ids, HEAD_BIT on each row's first edge.  id16 = 1:
+    // 16-bit ids relative to id_base (the split copies cut the sources into blocks of at most
+    // 32,768 ids), bit 15 marking each row's first edge.
+    int id16;
+    long long id_base;
+    // Staged launches (sweep_kernel_staged): the `src_rows` single-element source rows from `src`
+    // are copied into shared memory first and gathered from there; ids are relative to `src`.
+    long long src_rows;
 };
+
+// Edge id e of a chunk as stored (32-bit, or 16-bit zero-extended).  The load is issued a step
+// ahead of its use; decode_id turns it into the 32-bit form the sweep works with (source id |
+// HEAD_BIT) only when the step that needs it starts, so the warp does not wait for the load early.
+template <typename S> __device__ __forceinline__ uint32_t load_id(const SweepParams<S>& p, long long e) {
+    return p.id16 ? static_cast<uint32_t>(__ldg(reinterpret_cast<const unsigned short*>(p.adj) + e))
+                  : __ldg(p.adj + e);
+}
+template <typename S> __device__ __forceinline__ uint32_t decode_id(const SweepParams<S>& p, uint32_t r) {
+    return p.id16 ? (((r & 0x8000u) << 16) | (static_cast<uint32_t>(p.id_base) + (r & 0x7fffu))) : r;
+}
 
 template <typename S, int VW> struct Vec;
 template <> struct Vec<uint32_t, 1> { static __device__ __forceinline__ void ld(const uint32_t* p, uint32_t* v) { v[0] = __ldg(p); } static __device__ __forceinline__ void st(uint32_t* p, const uint32_t* v) { p[0] = v[0]; } };
@@ -154,6 +173,68 @@ template <> struct ChainTraits<AddF64S> {
     static constexpr bool kChains = true;
 };
 
+// Edge-id ring of a staged warp (16-bit ids): kRingStages steps of 256 ids in flight, each step's
+// ids copied global -> shared by cp.async (16 bytes per lane, 16-byte aligned, so a step's copy
+// starts up to 7 ids early and spans kRingIds ids).  The split copies are padded by kRingIds ids
+// so the last step's copy stays inside the allocation.
+constexpr int kRingStages = 4;
+constexpr int kRingIds = 256 + 8;
+constexpr int kRingWarpBytes = kRingStages * kRingIds * 2;
+
+__device__ __forceinline__ void ring_issue(unsigned short* slot, const unsigned short* adj16, long long abase,
+                                           int lane) {
+    const unsigned dst = static_cast<unsigned>(__cvta_generic_to_shared(slot + 8 * lane));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(adj16 + abase + 8 * lane) : "memory");
+    if (lane == 0) {
+        const unsigned d2 = static_cast<unsigned>(__cvta_generic_to_shared(slot + 256));
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d2), "l"(adj16 + abase + 256) : "memory");
+    }
+}
+__device__ __forceinline__ void ring_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N> __device__ __forceinline__ void ring_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// Chunk tail: the warp's last row sum is written, or -- a piece of a heavy row -- published as a
+// partial; the last piece to finish (atomic ticket) adds all of them up in piece order.
+template <class Op, int VW, int G>
+__device__ __forceinline__ void finish_chunk(const SweepParams<typename Op::S>& p, long long c, const ChunkDev& ch,
+                                             long long cur, VecAcc<Op, VW>& acc, int lane, int lg, int col,
+                                             bool colok) {
+    using A = typename Op::A;
+    constexpr int NG = 32 / G;
+    group_allreduce<Op, VW, G>(acc);
+    if (ch.heavy < 0) {
+        if (lg == 0 && colok) write_row<Op, VW>(p, cur, col, acc);
+        return;
+    }
+    const HeavyDev hr = p.heavy[ch.heavy];
+    const long long piece = c - hr.first_chunk;
+    A* part = reinterpret_cast<A*>(p.partials);
+    if (lg == 0 && colok) {
+#pragma unroll
+        for (int i = 0; i < VW; i++) part[(hr.slot_base + piece) * p.stride + col + i] = acc.get(i);
+    }
+    __threadfence();
+    __syncwarp();
+    unsigned ticket = 0;
+    if (lane == 0) ticket = atomicAdd(p.tickets + (long long)ch.heavy * p.ntiles + blockIdx.y, 1u);
+    ticket = __shfl_sync(FULL_MASK, ticket, 0);
+    if (ticket != (unsigned)hr.n_pieces - 1u) return;
+    __threadfence();
+    VecAcc<Op, VW> sum;
+    sum.zero();
+    if (colok) {
+        for (int pc = lg; pc < hr.n_pieces; pc += NG) {
+            const A* src = part + (hr.slot_base + pc) * p.stride + col;
+#pragma unroll
+            for (int i = 0; i < VW; i++) sum.add_partial(i, ld_cg(src + i));
+        }
+    }
+    group_allreduce<Op, VW, G>(sum);
+    if (lg == 0 && colok) write_row<Op, VW>(p, cur, col, sum);
+}
+
 template <class Op, int VW, int G, int D>
 __device__ __forceinline__ void sweep_chunk(const SweepParams<typename Op::S>& p, long long c, int lane) {
     using S = typename Op::S;
@@ -187,7 +268,7 @@ __device__ __forceinline__ void sweep_chunk(const SweepParams<typename Op::S>& p
 #pragma unroll
     for (int b = 0; b < UNR; b++) {
         const long long e = ch.e0 + 32 * b + lane;
-        nraw[b] = (e < eEnd) ? __ldg(p.adj + e) : 0u;
+        nraw[b] = (e < eEnd) ? load_id(p, e) : 0u;
     }
     for (long long base = ch.e0; base < eEnd; base += 32 * UNR) {
         uint32_t raw[UNR];
@@ -195,7 +276,7 @@ __device__ __forceinline__ void sweep_chunk(const SweepParams<typename Op::S>& p
         unsigned anyHead = 0;
 #pragma unroll
         for (int b = 0; b < UNR; b++) {
-            raw[b] = nraw[b];
+            raw[b] = decode_id(p, nraw[b]);
             heads[b] = __ballot_sync(FULL_MASK, raw[b] & 0x80000000u);
             anyHead |= heads[b];
         }
@@ -205,7 +286,7 @@ __device__ __forceinline__ void sweep_chunk(const SweepParams<typename Op::S>& p
 #pragma unroll
             for (int b = 0; b < UNR; b++) {
                 const long long e = nbase + 32 * b + lane;
-                nraw[b] = (e < eEnd) ? __ldg(p.adj + e) : 0u;
+                nraw[b] = (e < eEnd) ? load_id(p, e) : 0u;
             }
         }
         if (first) {
@@ -282,37 +363,116 @@ __device__ __forceinline__ void sweep_chunk(const SweepParams<typename Op::S>& p
         }
     }
 
-    group_allreduce<Op, VW, G>(acc);
-    if (ch.heavy < 0) {
-        if (lg == 0 && colok) write_row<Op, VW>(p, cur, col, acc);
-        return;
-    }
-    // Piece of a heavy row: publish the partial, then the last piece combines all of them.
-    const HeavyDev hr = p.heavy[ch.heavy];
-    const long long piece = c - hr.first_chunk;
-    A* part = reinterpret_cast<A*>(p.partials);
-    if (lg == 0 && colok) {
+    finish_chunk<Op, VW, G>(p, c, ch, cur, acc, lane, lg, col, colok);
+}
+
+// One chunk of a staged single-column split block (sweep_kernel_staged): the same row logic as
+// sweep_chunk with one lane per edge (G = 1, VW = 1), specialised for the short instruction path
+// this shape allows -- 16-bit block-relative ids read from the warp's cp.async ring, gathers from
+// the staged values by a 15-bit index, validity checks only in a chunk's last (partial) step.
+template <class Op>
+__device__ __forceinline__ void staged_chunk(const SweepParams<typename Op::S>& p, long long c, int lane,
+                                             const typename Op::S* __restrict__ staged, unsigned short* ring) {
+    using S = typename Op::S;
+    using Acc = VecAcc<Op, 1>;
+    constexpr int UNR = 8;  // 32-edge blocks per 256-edge step
+    const unsigned upto = (2u << lane) - 1u;  // lanes 0..lane
+    const ChunkDev ch = p.chunks[c];
+    const long long eEnd = p.chunks[c + 1].e0;
+    const unsigned short* adj16 = reinterpret_cast<const unsigned short*>(p.adj);
+    const int ringOff = static_cast<int>(ch.e0 & 7);  // ring copies start at the 16-byte boundary below e0
+    // the first kRingStages steps (a group is committed even when empty, to keep the count)
 #pragma unroll
-        for (int i = 0; i < VW; i++) part[(hr.slot_base + piece) * p.stride + col + i] = acc.get(i);
+    for (int st = 0; st < kRingStages; st++) {
+        const long long sb = ch.e0 + 256LL * st;
+        if (sb < eEnd) ring_issue(ring + st * kRingIds, adj16, sb - ringOff, lane);
+        ring_commit();
     }
-    __threadfence();
-    __syncwarp();
-    unsigned ticket = 0;
-    if (lane == 0) ticket = atomicAdd(p.tickets + (long long)ch.heavy * p.ntiles + blockIdx.y, 1u);
-    ticket = __shfl_sync(FULL_MASK, ticket, 0);
-    if (ticket != (unsigned)hr.n_pieces - 1u) return;
-    __threadfence();
-    Acc sum;
-    sum.zero();
-    if (colok) {
-        for (int pc = lg; pc < hr.n_pieces; pc += NG) {
-            const A* src = part + (hr.slot_base + pc) * p.stride + col;
+    Acc acc;
+    acc.zero();
+    long long cur = ch.r0;
+    bool first = true;
+    int step = 0;
+    for (long long base = ch.e0; base < eEnd; base += 256, step++) {
+        // this step's ids have landed (at most kRingStages - 1 later groups pending): read them,
+        // then refill the slot with the step kRingStages ahead
+        ring_wait<kRingStages - 1>();
+        __syncwarp();
+        unsigned short* slot = ring + (step % kRingStages) * kRingIds;
+        uint32_t r[UNR];
 #pragma unroll
-            for (int i = 0; i < VW; i++) sum.add_partial(i, ld_cg(src + i));
+        for (int b = 0; b < UNR; b++) r[b] = slot[ringOff + 32 * b + lane];
+        __syncwarp();
+        {
+            const long long sb = base + 256LL * kRingStages;
+            if (sb < eEnd) ring_issue(slot, adj16, sb - ringOff, lane);
+            ring_commit();
+        }
+        const long long left = eEnd - base;
+        S v[UNR][1];
+        if (left >= 256) {
+#pragma unroll
+            for (int b = 0; b < UNR; b++) v[b][0] = staged[r[b] & 0x7fffu];
+        } else {
+#pragma unroll
+            for (int b = 0; b < UNR; b++) {
+                const bool ok = 32 * b + lane < left;
+                if (!ok) r[b] = 0u;  // past the chunk: no row start, adds nothing
+                v[b][0] = ok ? staged[r[b] & 0x7fffu] : S{};
+            }
+        }
+        unsigned heads[UNR];
+        unsigned anyHead = 0;
+#pragma unroll
+        for (int b = 0; b < UNR; b++) {
+            heads[b] = __ballot_sync(FULL_MASK, r[b] & 0x8000u);
+            anyHead |= heads[b];
+        }
+        if (first) {
+            cur = ch.r0 - (long long)(heads[0] & 1u);
+            first = false;
+        }
+        if (anyHead == 0u) {
+            acc.template add_block<UNR>(v);
+            continue;
+        }
+#pragma unroll
+        for (int u = 0; u < UNR; u++) {
+            const unsigned hs = heads[u];
+            if (hs == 0u) {
+                acc.add(v[u]);
+                continue;
+            }
+            const int q = __popc(hs & upto);  // rows started at or before my edge
+            const int Q = __popc(hs);
+            // the current row ends in this 32-edge block
+            Acc x = acc;
+            if (q == 0) x.add(v[u]);
+            group_allreduce<Op, 1, 1>(x);
+            if (cur >= ch.r0 && lane == 0) write_row<Op, 1>(p, cur, 0, x);
+            // rows that start and end inside the block: segmented scan over the lanes
+            if (Q > 1) {
+                Acc y;
+                y.zero();
+                if (q >= 1) y.add(v[u]);
+#pragma unroll
+                for (int d = 1; d < 32; d <<= 1) {
+                    const int qu = __shfl_up_sync(FULL_MASK, q, d);
+                    const auto tv = y.shfl_up(d);
+                    if (lane >= d && qu == q) y.merge(tv);
+                }
+                const int qn = __shfl_down_sync(FULL_MASK, q, 1);
+                const bool tail = (lane == 31) || (qn != q);
+                if (tail && q >= 1 && q < Q) write_row<Op, 1>(p, cur + q, 0, y);
+            }
+            // the last row continues into the next block
+            acc.zero();
+            if (q == Q) acc.add(v[u]);
+            cur += Q;
         }
     }
-    group_allreduce<Op, VW, G>(sum);
-    if (lg == 0 && colok) write_row<Op, VW>(p, cur, col, sum);
+    ring_wait<0>();  // no copy into the ring outlives its chunk
+    finish_chunk<Op, 1, 1>(p, c, ch, cur, acc, lane, lane, 0, true);
 }
 
 // Persistent warps: each warp takes chunks of the level from a shared counter until none are
@@ -337,6 +497,64 @@ __global__ void __launch_bounds__(256, SweepOccupancy<Op, VW, G, D>::kBlocks) sw
         c = __shfl_sync(FULL_MASK, c, 0) + p.c_begin;
         if (c >= p.c_end) return;
         sweep_chunk<Op, VW, G, D>(p, c, lane);
+    }
+}
+
+// Single-column (stride 1) sweep of one split block whose source rows fit in shared memory:
+// every block of threads first copies the block's `src_rows` source values (p.src onwards, at
+// most kStagedRows of them) into shared memory, then its warps take chunks as above and gather
+// from there, each warp streaming its 16-bit edge ids through a cp.async ring behind the staged
+// values.  One 1024-thread block per SM: staged values and rings take most of the shared memory
+// (kStagedBytes<S>).
+constexpr int kStagedThreads = 1024;
+constexpr long long kStagedRows = 32768;
+template <typename S> constexpr int kStagedBytes = static_cast<int>(kStagedRows * sizeof(S)) +
+                                                    (kStagedThreads / 32) * kRingWarpBytes;
+template <class Op>
+__global__ void __launch_bounds__(kStagedThreads, 1) sweep_kernel_staged(const SweepParams<typename Op::S> p) {
+    using S = typename Op::S;
+    if (p.gate != nullptr && *p.gate != p.gate_value) return;
+    extern __shared__ __align__(16) unsigned char staged_raw[];
+    S* staged = reinterpret_cast<S*>(staged_raw);
+    unsigned short* ring = reinterpret_cast<unsigned short*>(staged_raw + kStagedRows * sizeof(S)) +
+                           (threadIdx.x >> 5) * (kRingWarpBytes / 2);
+    const long long rows = p.src_rows;  // <= kStagedRows, checked by the launcher
+    // 16-byte loads, all of a thread's issued before the first store (at most 8 per thread), and
+    // the source's unaligned head and tail element by element
+    const long long head = (16 - (reinterpret_cast<uintptr_t>(p.src) & 15)) / sizeof(S) % (16 / sizeof(S));
+    const long long nvec = (rows > head) ? (rows - head) / (16 / sizeof(S)) : 0;
+    const uint4* vsrc = reinterpret_cast<const uint4*>(p.src + head);
+    uint4 buf[8];
+#pragma unroll
+    for (int u = 0; u < 8; u++) {
+        const long long v = threadIdx.x + (long long)u * blockDim.x;
+        if (v < nvec) buf[u] = __ldg(vsrc + v);
+    }
+#pragma unroll
+    for (int u = 0; u < 8; u++) {
+        const long long v = threadIdx.x + (long long)u * blockDim.x;
+        if (v < nvec) {
+            const S* t = reinterpret_cast<const S*>(&buf[u]);
+#pragma unroll
+            for (int k = 0; k < (int)(16 / sizeof(S)); k++) staged[head + v * (16 / sizeof(S)) + k] = t[k];
+        }
+    }
+    for (long long v = threadIdx.x + 8LL * blockDim.x; v < nvec; v += blockDim.x) {  // (none at 1024 threads)
+        const uint4 t4 = __ldg(vsrc + v);
+        const S* t = reinterpret_cast<const S*>(&t4);
+        for (int k = 0; k < (int)(16 / sizeof(S)); k++) staged[head + v * (16 / sizeof(S)) + k] = t[k];
+    }
+    for (long long i = threadIdx.x; i < rows; i += blockDim.x)
+        if (i < head || i >= head + nvec * (long long)(16 / sizeof(S))) staged[i] = __ldg(p.src + i);
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    unsigned* counter = p.work + blockIdx.y;
+    for (;;) {
+        long long c = 0;
+        if (lane == 0) c = (long long)atomicAdd(counter, 1u);
+        c = __shfl_sync(FULL_MASK, c, 0) + p.c_begin;
+        if (c >= p.c_end) return;
+        staged_chunk<Op>(p, c, lane, staged, ring);
     }
 }
 

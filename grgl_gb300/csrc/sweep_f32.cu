@@ -8,4 +8,5 @@ void launch_sweep_f32(const SweepParams<float>& p, int vw, int g, int variant, d
     GRGX_SWEEP_DEEP4(AddF32)
     GRGX_SWEEP_UNSUPPORTED
 }
+void launch_sweep_staged_f32(const SweepParams<float>& p, dim3 grid, cudaStream_t s) GRGX_SWEEP_STAGED(AddF32)
 }  // namespace grgx

@@ -59,3 +59,12 @@
     GRGX_SWEEP_CASE(OP, 2, 32, 2)
 
 #define GRGX_SWEEP_UNSUPPORTED throw std::runtime_error("unsupported sweep shape");
+
+// The staged kernel with the block's source values as dynamic shared memory (opted in above the
+// default 48 KB on the current device on every launch: the call is cheap and per device).
+#define GRGX_SWEEP_STAGED(OP)                                                                      \
+    {                                                                                             \
+        const int bytes = kStagedBytes<typename OP::S>;                                            \
+        cudaFuncSetAttribute(sweep_kernel_staged<OP>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes); \
+        sweep_kernel_staged<OP><<<grid, kStagedThreads, bytes, s>>>(p);                            \
+    }

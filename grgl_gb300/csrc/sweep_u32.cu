@@ -8,4 +8,5 @@ void launch_sweep_u32(const SweepParams<uint32_t>& p, int vw, int g, int variant
     GRGX_SWEEP_DEEP4(AddU32)
     GRGX_SWEEP_UNSUPPORTED
 }
+void launch_sweep_staged_u32(const SweepParams<uint32_t>& p, dim3 grid, cudaStream_t s) GRGX_SWEEP_STAGED(AddU32)
 }  // namespace grgx
