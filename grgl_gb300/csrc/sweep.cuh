@@ -65,12 +65,14 @@ template <typename S> struct SweepParams {
 // Edge id e of a chunk as stored (32-bit, or 16-bit zero-extended).  The load is issued a step
 // ahead of its use; decode_id turns it into the 32-bit form the sweep works with (source id |
 // HEAD_BIT) only when the step that needs it starts, so the warp does not wait for the load early.
-template <typename S> __device__ __forceinline__ uint32_t load_id(const SweepParams<S>& p, long long e) {
-    return p.id16 ? static_cast<uint32_t>(__ldg(reinterpret_cast<const unsigned short*>(p.adj) + e))
-                  : __ldg(p.adj + e);
+// The id width is a template parameter (ID16 = p.id16), so the 32-bit kernels carry no 16-bit code.
+template <bool ID16, typename S> __device__ __forceinline__ uint32_t load_id(const SweepParams<S>& p, long long e) {
+    if constexpr (ID16) return static_cast<uint32_t>(__ldg(reinterpret_cast<const unsigned short*>(p.adj) + e));
+    else return __ldg(p.adj + e);
 }
-template <typename S> __device__ __forceinline__ uint32_t decode_id(const SweepParams<S>& p, uint32_t r) {
-    return p.id16 ? (((r & 0x8000u) << 16) | (static_cast<uint32_t>(p.id_base) + (r & 0x7fffu))) : r;
+template <bool ID16, typename S> __device__ __forceinline__ uint32_t decode_id(const SweepParams<S>& p, uint32_t r) {
+    if constexpr (ID16) return ((r & 0x8000u) << 16) | (static_cast<uint32_t>(p.id_base) + (r & 0x7fffu));
+    else return r;
 }
 
 template <typename S, int VW> struct Vec;
@@ -235,7 +237,7 @@ __device__ __forceinline__ void finish_chunk(const SweepParams<typename Op::S>& 
     if (lg == 0 && colok) write_row<Op, VW>(p, cur, col, sum);
 }
 
-template <class Op, int VW, int G, int D>
+template <class Op, int VW, int G, int D, bool ID16>
 __device__ __forceinline__ void sweep_chunk(const SweepParams<typename Op::S>& p, long long c, int lane) {
     using S = typename Op::S;
     using A = typename Op::A;
@@ -268,7 +270,7 @@ __device__ __forceinline__ void sweep_chunk(const SweepParams<typename Op::S>& p
 #pragma unroll
     for (int b = 0; b < UNR; b++) {
         const long long e = ch.e0 + 32 * b + lane;
-        nraw[b] = (e < eEnd) ? load_id(p, e) : 0u;
+        nraw[b] = (e < eEnd) ? load_id<ID16>(p, e) : 0u;
     }
     for (long long base = ch.e0; base < eEnd; base += 32 * UNR) {
         uint32_t raw[UNR];
@@ -276,7 +278,7 @@ __device__ __forceinline__ void sweep_chunk(const SweepParams<typename Op::S>& p
         unsigned anyHead = 0;
 #pragma unroll
         for (int b = 0; b < UNR; b++) {
-            raw[b] = decode_id(p, nraw[b]);
+            raw[b] = decode_id<ID16>(p, nraw[b]);
             heads[b] = __ballot_sync(FULL_MASK, raw[b] & 0x80000000u);
             anyHead |= heads[b];
         }
@@ -286,7 +288,7 @@ __device__ __forceinline__ void sweep_chunk(const SweepParams<typename Op::S>& p
 #pragma unroll
             for (int b = 0; b < UNR; b++) {
                 const long long e = nbase + 32 * b + lane;
-                nraw[b] = (e < eEnd) ? load_id(p, e) : 0u;
+                nraw[b] = (e < eEnd) ? load_id<ID16>(p, e) : 0u;
             }
         }
         if (first) {
@@ -486,7 +488,7 @@ template <class Op, int VW, int G, int D> struct SweepOccupancy {
     static constexpr int kBlocks = (kWide ? 3 : 4) - (D > 1 ? 1 : 0);
 };
 
-template <class Op, int VW, int G, int D>
+template <class Op, int VW, int G, int D, bool ID16>
 __global__ void __launch_bounds__(256, SweepOccupancy<Op, VW, G, D>::kBlocks) sweep_kernel(const SweepParams<typename Op::S> p) {
     if (p.gate != nullptr && *p.gate != p.gate_value) return;
     const int lane = threadIdx.x & 31;
@@ -496,7 +498,7 @@ __global__ void __launch_bounds__(256, SweepOccupancy<Op, VW, G, D>::kBlocks) sw
         if (lane == 0) c = (long long)atomicAdd(counter, 1u);
         c = __shfl_sync(FULL_MASK, c, 0) + p.c_begin;
         if (c >= p.c_end) return;
-        sweep_chunk<Op, VW, G, D>(p, c, lane);
+        sweep_chunk<Op, VW, G, D, ID16>(p, c, lane);
     }
 }
 

@@ -5,18 +5,22 @@
 
 #include "launch.h"
 
-// Persistent grid: at most as many blocks as can be resident at once.
+// Persistent grid: at most as many blocks as can be resident at once.  The 16-bit-id instance
+// (split block passes) and the 32-bit one are separate kernels.
 #define GRGX_SWEEP_CASE(OP, VWV, GV, DV)                                              \
     if (vw == VWV && g == GV && variant == DV - 1) {                                  \
         static int perSm = 0;                                                         \
         if (perSm == 0) {                                                             \
             int nb = 0;                                                               \
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, sweep_kernel<OP, VWV, GV, DV>, 256, 0); \
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, sweep_kernel<OP, VWV, GV, DV, false>, 256, 0); \
             perSm = nb > 0 ? nb : 1;                                                  \
         }                                                                             \
         const unsigned cap = (unsigned)(perSm * sms);                                 \
         if (grid.x > cap) grid.x = cap;                                               \
-        sweep_kernel<OP, VWV, GV, DV><<<grid, 256, 0, s>>>(p);                        \
+        if (p.id16)                                                                   \
+            sweep_kernel<OP, VWV, GV, DV, true><<<grid, 256, 0, s>>>(p);              \
+        else                                                                          \
+            sweep_kernel<OP, VWV, GV, DV, false><<<grid, 256, 0, s>>>(p);             \
         return;                                                                       \
     }
 
