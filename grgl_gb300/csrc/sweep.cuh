@@ -103,7 +103,7 @@ template <typename S, int VW> __device__ __forceinline__ void ld_plain(const S* 
 }
 
 // Sum of a lane's accumulator over the 32/G groups of the warp (every group gets the result).
-template <class Op, int VW, int G> __device__ __forceinline__ void group_allreduce(VecAcc<Op, VW>& x) {
+template <class Op, int VW, int G, class Acc> __device__ __forceinline__ void group_allreduce(Acc& x) {
 #pragma unroll
     for (int m = G; m < 32; m <<= 1) {
         const auto t = x.shfl_xor(m);
@@ -127,9 +127,9 @@ __device__ __forceinline__ F32Pair ld_cg(const F32Pair* p) {
     return {t.x, t.y};
 }
 
-template <class Op, int VW>
+template <class Op, int VW, class Acc>
 __device__ __forceinline__ void write_row(const SweepParams<typename Op::S>& p, long long row, int col,
-                                          const VecAcc<Op, VW>& tot) {
+                                          const Acc& tot) {
     using S = typename Op::S;
     using A = typename Op::A;
     const long long node = p.rows[row];
@@ -199,10 +199,9 @@ template <int N> __device__ __forceinline__ void ring_wait() {
 
 // Chunk tail: the warp's last row sum is written, or -- a piece of a heavy row -- published as a
 // partial; the last piece to finish (atomic ticket) adds all of them up in piece order.
-template <class Op, int VW, int G>
+template <class Op, int VW, int G, class Acc>
 __device__ __forceinline__ void finish_chunk(const SweepParams<typename Op::S>& p, long long c, const ChunkDev& ch,
-                                             long long cur, VecAcc<Op, VW>& acc, int lane, int lg, int col,
-                                             bool colok) {
+                                             long long cur, Acc& acc, int lane, int lg, int col, bool colok) {
     using A = typename Op::A;
     constexpr int NG = 32 / G;
     group_allreduce<Op, VW, G>(acc);
@@ -224,7 +223,7 @@ __device__ __forceinline__ void finish_chunk(const SweepParams<typename Op::S>& 
     ticket = __shfl_sync(FULL_MASK, ticket, 0);
     if (ticket != (unsigned)hr.n_pieces - 1u) return;
     __threadfence();
-    VecAcc<Op, VW> sum;
+    Acc sum;
     sum.zero();
     if (colok) {
         for (int pc = lg; pc < hr.n_pieces; pc += NG) {
@@ -376,7 +375,9 @@ template <class Op>
 __device__ __forceinline__ void staged_chunk(const SweepParams<typename Op::S>& p, long long c, int lane,
                                              const typename Op::S* __restrict__ staged, unsigned short* ring) {
     using S = typename Op::S;
-    using Acc = VecAcc<Op, 1>;
+    // one scalar accumulator per lane (ScalarAcc: the packed two-half form of compensated float32
+    // needs registers this 1024-thread kernel does not have)
+    using Acc = ScalarAcc<Op, 1>;
     constexpr int UNR = 8;  // 32-edge blocks per 256-edge step
     const unsigned upto = (2u << lane) - 1u;  // lanes 0..lane
     const ChunkDev ch = p.chunks[c];
@@ -423,20 +424,21 @@ __device__ __forceinline__ void staged_chunk(const SweepParams<typename Op::S>& 
                 v[b][0] = ok ? staged[r[b] & 0x7fffu] : S{};
             }
         }
-        unsigned heads[UNR];
-        unsigned anyHead = 0;
+        // one ballot tells whether any row starts in the step; only then the per-block ones
+        uint32_t orAll = 0;
 #pragma unroll
-        for (int b = 0; b < UNR; b++) {
-            heads[b] = __ballot_sync(FULL_MASK, r[b] & 0x8000u);
-            anyHead |= heads[b];
+        for (int b = 0; b < UNR; b++) orAll |= r[b];
+        if (__ballot_sync(FULL_MASK, orAll & 0x8000u) == 0u) {
+            first = false;  // the chunk's first edge continues a row: cur = ch.r0
+            acc.template add_block<UNR>(v);
+            continue;
         }
+        unsigned heads[UNR];
+#pragma unroll
+        for (int b = 0; b < UNR; b++) heads[b] = __ballot_sync(FULL_MASK, r[b] & 0x8000u);
         if (first) {
             cur = ch.r0 - (long long)(heads[0] & 1u);
             first = false;
-        }
-        if (anyHead == 0u) {
-            acc.template add_block<UNR>(v);
-            continue;
         }
 #pragma unroll
         for (int u = 0; u < UNR; u++) {

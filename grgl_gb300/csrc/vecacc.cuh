@@ -28,7 +28,9 @@ __device__ __forceinline__ void two_sum2(float2 a, float2 b, float2& s, float2& 
     e = add2(sub2(a, sub2(s, bb)), sub2(b, bb));
 }
 
-template <class Op, int VW> struct VecAcc {
+// One Op::A accumulator per column (the generic accumulator; also used directly where a kernel
+// wants the scalar form of a type VecAcc specialises).
+template <class Op, int VW> struct ScalarAcc {
     using S = typename Op::S;
     using A = typename Op::A;
     A a[VW];
@@ -45,24 +47,90 @@ template <class Op, int VW> struct VecAcc {
 #pragma unroll
         for (int u = 0; u < N; u++) add(v[u]);
     }
-    __device__ __forceinline__ void merge(const VecAcc& o) {
+    __device__ __forceinline__ void merge(const ScalarAcc& o) {
 #pragma unroll
         for (int i = 0; i < VW; i++) Op::merge(a[i], o.a[i]);
     }
-    __device__ __forceinline__ VecAcc shfl_xor(int m) const {
-        VecAcc r;
+    __device__ __forceinline__ ScalarAcc shfl_xor(int m) const {
+        ScalarAcc r;
 #pragma unroll
         for (int i = 0; i < VW; i++) r.a[i] = Op::shfl_xor(a[i], m);
         return r;
     }
-    __device__ __forceinline__ VecAcc shfl_up(int d) const {
-        VecAcc r;
+    __device__ __forceinline__ ScalarAcc shfl_up(int d) const {
+        ScalarAcc r;
 #pragma unroll
         for (int i = 0; i < VW; i++) r.a[i] = Op::shfl_up(a[i], d);
         return r;
     }
     __device__ __forceinline__ A get(int i) const { return a[i]; }
     __device__ __forceinline__ void add_partial(int i, const A& x) { Op::merge(a[i], x); }
+    __device__ __forceinline__ void settle() {}
+    __device__ __forceinline__ void flush() {}
+};
+
+template <class Op, int VW> struct VecAcc : ScalarAcc<Op, VW> {
+    __device__ __forceinline__ VecAcc() = default;
+    __device__ __forceinline__ VecAcc(const ScalarAcc<Op, VW>& s) : ScalarAcc<Op, VW>(s) {}
+    __device__ __forceinline__ VecAcc shfl_xor(int m) const { return VecAcc(ScalarAcc<Op, VW>::shfl_xor(m)); }
+    __device__ __forceinline__ VecAcc shfl_up(int d) const { return VecAcc(ScalarAcc<Op, VW>::shfl_up(d)); }
+};
+
+// Compensated float32, one column (K = 1): two independent compensated partial sums in the .x
+// and .y halves of float2 registers, so a boundary-free step adds its edges two at a time with
+// packed TwoSums (FADD2); single adds go to .x.  get() merges the halves (one more TwoSum), and
+// merges, shuffles and partials work half by half.  Per node the error stays that of a
+// compensated sum: each half's running error is carried exactly until the final merge.
+template <> struct VecAcc<AddF32C, 1> {
+    using S = float;
+    using A = F32Pair;
+    float2 hi, lo;
+    __device__ __forceinline__ void zero() { hi = lo = make_float2(0.0f, 0.0f); }
+    __device__ __forceinline__ void add(const float* v) {
+        A x{hi.x, lo.x};
+        AddF32C::add(x, v[0]);
+        hi.x = x.hi;
+        lo.x = x.lo;
+    }
+    template <int N> __device__ __forceinline__ void add_block(const float (*v)[1]) {
+#pragma unroll
+        for (int u = 0; u + 1 < N; u += 2) {
+            float2 sum, err;
+            two_sum2(hi, make_float2(v[u][0], v[u + 1][0]), sum, err);
+            hi = sum;
+            lo = add2(lo, err);
+        }
+        if (N & 1) add(v[N - 1]);
+    }
+    __device__ __forceinline__ void merge(const VecAcc& o) {
+        float2 sum, err;
+        two_sum2(hi, o.hi, sum, err);
+        hi = sum;
+        lo = add2(lo, add2(o.lo, err));
+    }
+    __device__ __forceinline__ VecAcc shfl_xor(int m) const {
+        VecAcc r;
+        r.hi = shfl_xor2(hi, m);
+        r.lo = shfl_xor2(lo, m);
+        return r;
+    }
+    __device__ __forceinline__ VecAcc shfl_up(int d) const {
+        VecAcc r;
+        r.hi = shfl_up2(hi, d);
+        r.lo = shfl_up2(lo, d);
+        return r;
+    }
+    __device__ __forceinline__ A get(int) const {
+        A x{hi.x, lo.x};
+        AddF32C::merge(x, A{hi.y, lo.y});
+        return x;
+    }
+    __device__ __forceinline__ void add_partial(int, const A& p) {
+        A x{hi.x, lo.x};
+        AddF32C::merge(x, p);
+        hi.x = x.hi;
+        lo.x = x.lo;
+    }
     __device__ __forceinline__ void settle() {}
     __device__ __forceinline__ void flush() {}
 };
