@@ -629,7 +629,7 @@ def matmul_batch(grg: GRG, requests, max_cols: int = 0, *, f32_compensated: bool
     tensors.  A standardized request computes what ``matmul_standardized`` does; by_individual
     has ``matmul``'s meaning.  Returns the outputs in order.  Requests of the same direction
     and dtype are stacked into traversals of at most ``max_cols`` rows (0 = 512 for 4-byte and
-    smaller dtypes, 256 for 8-byte ones).
+    smaller dtypes, 256 for 8-byte ones); a request's rows may be cut across two traversals.
     """
     prepared = [_request_for(grg, r[0], r[1], bool(r[2]) if len(r) > 2 else False,
                              bool(r[3]) if len(r) > 3 else False) for r in requests]

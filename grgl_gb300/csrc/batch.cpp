@@ -114,29 +114,64 @@ void matmul_batch_impl(grgx_graph* g, const grgx_request* reqs, uint64_t n, uint
     }
     const uint32_t passFlags = (flags & (GRGX_FLAG_F32_PLAIN | GRGX_FLAG_F64_NATIVE)) | GRGX_FLAG_DEVICE_POINTERS |
                                GRGX_FLAG_OVERWRITE;
-    // The stacks: per group, requests in order while the stacked rows fit `width` (a wider
-    // request runs alone).
+    // The stacks: per group, the requests' rows in submission order cut into stacks of `width`
+    // rows (a request may span two stacks: its rows are independent products).  A traversal
+    // covers a row in column tiles of 32 lanes x 16 bytes (128 four-byte or 64 eight-byte
+    // columns), and a tile costs nearly a full pass however few of its columns are used; so when
+    // a group's last stack would end in a tile less than a quarter full, those rows run as a
+    // stack of their own with a narrow layout instead.
+    struct Piece {
+        uint64_t req, r0, r1;  // rows r0 .. r1 of request req
+    };
     struct Stack {
         int direction, dtype, byIndiv;
-        std::vector<uint64_t> req;
+        std::vector<Piece> pieces;
         uint64_t rows;
     };
     std::vector<Stack> stacks;
     for (auto& kv : groups) {
         const int direction = std::get<0>(kv.first), dtype = std::get<1>(kv.first), byIndiv = std::get<2>(kv.first);
         const uint64_t width = maxCols ? maxCols : default_batch_cols(dtype);
-        const std::vector<uint64_t>& idx = kv.second;
-        size_t i = 0;
-        while (i < idx.size()) {
-            Stack st{direction, dtype, byIndiv, {idx[i]}, reqs[idx[i]].rows};
-            size_t j = i + 1;
-            while (j < idx.size() && st.rows + reqs[idx[j]].rows <= width) {
-                st.rows += reqs[idx[j]].rows;
-                st.req.push_back(idx[j++]);
+        const uint64_t tile = (dtype == GRGX_BOOL) ? 0 : (elem_bytes(dtype) >= 8 ? 64 : 128);
+        std::vector<Stack> gs;
+        Stack cur{direction, dtype, byIndiv, {}, 0};
+        for (uint64_t k : kv.second) {
+            uint64_t r0 = 0;
+            const uint64_t rows = reqs[k].rows;
+            while (r0 < rows) {
+                const uint64_t take = std::min(rows - r0, width - cur.rows);
+                cur.pieces.push_back({k, r0, r0 + take});
+                cur.rows += take;
+                r0 += take;
+                if (cur.rows == width) {
+                    gs.push_back(std::move(cur));
+                    cur = Stack{direction, dtype, byIndiv, {}, 0};
+                }
             }
-            stacks.push_back(std::move(st));
-            i = j;
         }
+        if (cur.rows) {
+            const uint64_t rem = tile ? cur.rows % tile : 0;
+            if (tile && cur.rows > tile && rem > 0 && rem * 4 <= tile) {
+                // split the last `rem` rows off into their own stack
+                Stack tail{direction, dtype, byIndiv, {}, 0};
+                uint64_t need = rem;
+                while (need > 0) {
+                    Piece& pc = cur.pieces.back();
+                    const uint64_t take = std::min(need, pc.r1 - pc.r0);
+                    tail.pieces.insert(tail.pieces.begin(), Piece{pc.req, pc.r1 - take, pc.r1});
+                    pc.r1 -= take;
+                    if (pc.r1 == pc.r0) cur.pieces.pop_back();
+                    need -= take;
+                }
+                cur.rows -= rem;
+                tail.rows = rem;
+                gs.push_back(std::move(cur));
+                gs.push_back(std::move(tail));
+            } else {
+                gs.push_back(std::move(cur));
+            }
+        }
+        for (auto& st : gs) stacks.push_back(std::move(st));
     }
     // Several stacks: fork them over the batch streams (round robin, after the work already queued
     // on the caller's stream) and join them back onto it at the end.
@@ -157,21 +192,25 @@ void matmul_batch_impl(grgx_graph* g, const grgx_request* reqs, uint64_t n, uint
         const uint64_t cols = (direction == GRGX_DIRECTION_UP) ? sampleCols : hg.num_mutations;
         const uint64_t outCols = (direction == GRGX_DIRECTION_UP) ? hg.num_mutations : sampleCols;
         const size_t es = elem_bytes(dtype);
-        if (st.req.size() == 1) {
-            const grgx_request& r = reqs[st.req[0]];
+        if (st.pieces.size() == 1) {
+            // one piece: the request's own buffers (offset to its rows)
+            const Piece& pc = st.pieces[0];
+            const grgx_request& r = reqs[pc.req];
+            const uint64_t K = pc.r1 - pc.r0;
+            const void* inp = static_cast<const char*>(r.input) + pc.r0 * cols * es;
+            void* outp = static_cast<char*>(r.output) + pc.r0 * outCols * es;
             // host buffers on a batch stream are queued asynchronously; the join below orders them
             const uint32_t f = (flags & ~GRGX_FLAG_SYNC) | (nstreams > 1 && !dev ? GRGX_FLAG_ASYNC : 0u);
             if (r.options & GRGX_REQUEST_STANDARDIZED)
-                matmul_standardized_impl(g, dtype, r.input, cols, r.rows, direction, r.output, r.rows * outCols, f,
-                                         ss);
+                matmul_standardized_impl(g, dtype, inp, cols, K, direction, outp, K * outCols, f, ss);
             else
-                matmul_impl(g, dtype, r.input, cols, r.rows, direction, r.output, r.rows * outCols, 0, byIndiv,
-                            nullptr, GRGX_INIT_ZERO, nullptr, f | GRGX_FLAG_OVERWRITE, ss);
+                matmul_impl(g, dtype, inp, cols, K, direction, outp, K * outCols, 0, byIndiv, nullptr,
+                            GRGX_INIT_ZERO, nullptr, f | GRGX_FLAG_OVERWRITE, ss);
             continue;
         }
         const uint64_t rowsTotal = st.rows;
         bool anyStd = false;
-        for (uint64_t k : st.req) anyStd |= (reqs[k].options & GRGX_REQUEST_STANDARDIZED) != 0;
+        for (const Piece& pc : st.pieces) anyStd |= (reqs[pc.req].options & GRGX_REQUEST_STANDARDIZED) != 0;
         DevicePlan* dp = anyStd ? standardized_plan(g, ss) : nullptr;
         double* red = nullptr;
         if (anyStd) BATCH_CUDA(pool_malloc(reinterpret_cast<void**>(&red), rowsTotal * sizeof(double), ss));
@@ -180,34 +219,36 @@ void matmul_batch_impl(grgx_graph* g, const grgx_request* reqs, uint64_t n, uint
         BATCH_CUDA(pool_malloc(&in, rowsTotal * cols * es, ss));
         BATCH_CUDA(pool_malloc(&out, rowsTotal * outCols * es, ss));
         uint64_t row = 0;
-        for (uint64_t k : st.req) {
-            const grgx_request& r = reqs[k];
+        for (const Piece& pc : st.pieces) {
+            const grgx_request& r = reqs[pc.req];
+            const uint64_t K = pc.r1 - pc.r0;
             char* rowsIn = static_cast<char*>(in) + row * cols * es;
-            BATCH_CUDA(cudaMemcpyAsync(rowsIn, r.input, r.rows * cols * es,
+            BATCH_CUDA(cudaMemcpyAsync(rowsIn, static_cast<const char*>(r.input) + pc.r0 * cols * es, K * cols * es,
                                        dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, ss));
             if ((r.options & GRGX_REQUEST_STANDARDIZED) && direction == GRGX_DIRECTION_DOWN)
-                standardized_prepare_down(dtype, dp, rowsIn, static_cast<long long>(r.rows),
-                                          static_cast<long long>(cols), red + row, ss);
-            row += r.rows;
+                standardized_prepare_down(dtype, dp, rowsIn, static_cast<long long>(K), static_cast<long long>(cols),
+                                          red + row, ss);
+            row += K;
         }
         matmul_impl(g, dtype, in, cols, rowsTotal, direction, out, rowsTotal * outCols, 0, byIndiv, nullptr,
                     GRGX_INIT_ZERO, nullptr, passFlags, ss);
         row = 0;
-        for (uint64_t k : st.req) {
-            const grgx_request& r = reqs[k];
+        for (const Piece& pc : st.pieces) {
+            const grgx_request& r = reqs[pc.req];
+            const uint64_t K = pc.r1 - pc.r0;
             char* rowsOut = static_cast<char*>(out) + row * outCols * es;
             if (r.options & GRGX_REQUEST_STANDARDIZED) {
                 if (direction == GRGX_DIRECTION_DOWN)
-                    standardized_finish_down(dtype, rowsOut, red + row, static_cast<long long>(r.rows),
+                    standardized_finish_down(dtype, rowsOut, red + row, static_cast<long long>(K),
                                              static_cast<long long>(outCols), ss);
                 else
                     standardized_finish_up(dtype, dp, static_cast<char*>(in) + row * cols * es,
-                                           static_cast<long long>(r.rows), static_cast<long long>(cols), rowsOut,
+                                           static_cast<long long>(K), static_cast<long long>(cols), rowsOut,
                                            static_cast<long long>(outCols), red + row, ss);
             }
-            BATCH_CUDA(cudaMemcpyAsync(r.output, rowsOut, r.rows * outCols * es,
+            BATCH_CUDA(cudaMemcpyAsync(static_cast<char*>(r.output) + pc.r0 * outCols * es, rowsOut, K * outCols * es,
                                        dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, ss));
-            row += r.rows;
+            row += K;
         }
         BATCH_CUDA(cudaFreeAsync(in, ss));
         BATCH_CUDA(cudaFreeAsync(out, ss));

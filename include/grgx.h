@@ -201,7 +201,11 @@ typedef struct {
 /* No counterpart in the reference (its callers loop over matMul calls).  Runs `n` requests on
  * one graph with as few traversals as possible: requests of the same direction and dtype are
  * stacked row-wise into traversals of at most `max_cols` columns (0 = 512 four-byte or 256
- * eight-byte columns), so the edge stream and the launches are shared.  Each request's
+ * eight-byte columns), so the edge stream and the launches are shared; a request's rows may be
+ * cut across two traversals, and rows that would leave a group's last traversal with a nearly
+ * empty 128-column (64 for eight-byte values) tile run as a narrow traversal of their own.  The
+ * stacks run on up to three internal streams that join `stream` before the call's work is
+ * complete on it.  Each request's
  * result equals its own grgx_matmul result (bit-exact for integers; float sums may round
  * differently because the stacked row is wider).  Flags as grgx_matmul
  * (GRGX_FLAG_DEVICE_POINTERS, GRGX_FLAG_F32_PLAIN, GRGX_FLAG_F64_NATIVE). */

@@ -71,6 +71,23 @@ def test_matmul_batch_matches_single(gx, graphs, oracles):
         _check_same(gx, g, V, d, out.cpu().numpy())
 
 
+def test_matmul_batch_splits_rows_across_stacks(gx, graphs, oracles):
+    """Requests whose rows are cut across stacks (narrow stacking widths), and a group whose last
+    stack would end in a nearly empty column tile (136 four-byte rows: stacks of 128 and 8), give
+    each request's own product."""
+    g = graphs[0]
+    rng = np.random.default_rng(4)
+    reqs = [(_rand(rng, np.float32, (8, g.num_samples)), UP) for _ in range(17)]
+    reqs += [(_rand(rng, np.int64, (3, g.num_mutations)), DOWN) for _ in range(5)]
+    reqs += [(_rand(rng, np.int32, (70, g.num_mutations)), DOWN)]
+    for width in (0, 5, 64):
+        outs = gx.matmul_batch(g, reqs, max_cols=width)
+        for (V, d), out in zip(reqs, outs):
+            _check_same(gx, g, V, d, out)
+    assert_matches_oracle(oracles[0], reqs[0][0], UP, outs[0])
+    assert_matches_oracle(oracles[0], reqs[-1][0], DOWN, outs[-1])
+
+
 def test_server_results_alone_and_in_the_mix(gx, graphs, oracles):
     rng = np.random.default_rng(1)
     reqs = []
