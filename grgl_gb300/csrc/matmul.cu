@@ -206,6 +206,7 @@ SweepParams<S> make_params(const DevCSR& c, long long cb, long long ce, const vo
     p.id16 = 0;
     p.id_base = 0;
     p.src_rows = 0;
+    p.col_base = 0;
     return p;
 }
 
@@ -220,29 +221,52 @@ int launch_level(const Layout& L, const DevCSR& c, size_t level, const void* src
     const LevelShape sh = shape ? *shape : default_shape(L);
     const int ts = tileStride > 0 ? tileStride : L.ntiles;
     if (sh.ntiles > ts) throw Error(GRGX_ERR_CUDA, "launch shape has more column tiles than counters");
-    const dim3 grid(static_cast<unsigned>((ce - cb + 7) / 8), static_cast<unsigned>(sh.ntiles));
     const int sms = sm_count();
-    auto prm = [&](auto tag) {
-        using S = decltype(tag);
-        SweepParams<S> p = make_params<S>(c, cb, ce, src, dst, L.stride, rmw, partials, tickets, work, ts);
-        p.gate = gate;
-        p.gate_value = gateValue;
-        p.state = state;
-        p.state_base = stateBase;
-        p.state_mode = stateMode;
-        return p;
+    const long long base = c.id16 ? c.level_base[level] : 0;
+    // One launch of `tiles` column tiles of g lanes from column colBase; its work counters and
+    // heavy-row tickets are those of tile slot `slot` onwards.
+    auto launch = [&](int g, int tiles, int variant, int colBase, int slot) {
+        const dim3 grid(static_cast<unsigned>((ce - cb + 7) / 8), static_cast<unsigned>(tiles));
+        auto prm = [&](auto tag) {
+            using S = decltype(tag);
+            SweepParams<S> p = make_params<S>(c, cb, ce, src, dst, L.stride, rmw, partials, tickets + slot,
+                                              work + slot, ts);
+            p.gate = gate;
+            p.gate_value = gateValue;
+            p.state = state;
+            p.state_base = stateBase;
+            p.state_mode = stateMode;
+            p.col_base = colBase;
+            // a split block: 16-bit ids relative to the block's first source id
+            p.id16 = c.id16 ? 1 : 0;
+            p.id_base = base;
+            return p;
+        };
+        const int vw = L.vw;
+        switch (L.kind) {
+        case Kind::U32: launch_sweep_u32(prm(uint32_t{}), vw, g, variant, grid, sms, s); break;
+        case Kind::XOR: launch_sweep_xor(prm(uint32_t{}), vw, g, variant, grid, sms, s); break;
+        case Kind::U64: launch_sweep_u64(prm(static_cast<unsigned long long>(0)), vw, g, variant, grid, sms, s); break;
+        case Kind::F64: launch_sweep_f64(prm(double{}), vw, g, variant, grid, sms, s); break;
+        case Kind::F32C: launch_sweep_f32c(prm(float{}), vw, g, variant, grid, sms, s); break;
+        case Kind::F32: launch_sweep_f32(prm(float{}), vw, g, variant, grid, sms, s); break;
+        case Kind::F64S: launch_sweep_f64s(prm(DF{}), vw, g, variant, grid, sms, s); break;
+        }
     };
-    const int vw = L.vw, g = sh.g, v = sh.variant;
     if (c.id16) {
-        // a split block: 16-bit ids relative to the block's first source id.  Single-column
-        // 4-byte rows stage the block's sources in shared memory (one 1024-thread block per SM).
-        const long long base = c.level_base[level], srows = c.level_src_rows[level];
-        const bool staged = staged_layout(L) && srows <= kStagedRows && sh.ntiles == 1;
-        if (staged) {
+        // single-column 4-byte rows stage the block's sources in shared memory (one 1024-thread
+        // block per SM)
+        const long long srows = c.level_src_rows[level];
+        if (staged_layout(L) && srows <= kStagedRows && sh.ntiles == 1) {
             const dim3 sgrid(static_cast<unsigned>(std::min<long long>((ce - cb + 7) / 8, sms)), 1);
             auto sp = [&](auto tag) {
                 using S = decltype(tag);
-                SweepParams<S> p = prm(tag);
+                SweepParams<S> p = make_params<S>(c, cb, ce, src, dst, L.stride, rmw, partials, tickets, work, ts);
+                p.gate = gate;
+                p.gate_value = gateValue;
+                p.state = state;
+                p.state_base = stateBase;
+                p.state_mode = stateMode;
                 p.id16 = 1;
                 p.id_base = 0;
                 p.src = static_cast<const S*>(src) + base;
@@ -258,32 +282,19 @@ int launch_level(const Layout& L, const DevCSR& c, size_t level, const void* src
             }
             return 1;
         }
-        auto ip = [&](auto tag) {
-            auto p = prm(tag);
-            p.id16 = 1;
-            p.id_base = base;
-            return p;
-        };
-        switch (L.kind) {
-        case Kind::U32: launch_sweep_u32(ip(uint32_t{}), vw, g, v, grid, sms, s); break;
-        case Kind::XOR: launch_sweep_xor(ip(uint32_t{}), vw, g, v, grid, sms, s); break;
-        case Kind::U64: launch_sweep_u64(ip(static_cast<unsigned long long>(0)), vw, g, v, grid, sms, s); break;
-        case Kind::F64: launch_sweep_f64(ip(double{}), vw, g, v, grid, sms, s); break;
-        case Kind::F32C: launch_sweep_f32c(ip(float{}), vw, g, v, grid, sms, s); break;
-        case Kind::F32: launch_sweep_f32(ip(float{}), vw, g, v, grid, sms, s); break;
-        case Kind::F64S: launch_sweep_f64s(ip(DF{}), vw, g, v, grid, sms, s); break;
-        }
-        return 1;
     }
-    switch (L.kind) {
-    case Kind::U32: launch_sweep_u32(prm(uint32_t{}), vw, g, v, grid, sms, s); break;
-    case Kind::XOR: launch_sweep_xor(prm(uint32_t{}), vw, g, v, grid, sms, s); break;
-    case Kind::U64: launch_sweep_u64(prm(static_cast<unsigned long long>(0)), vw, g, v, grid, sms, s); break;
-    case Kind::F64: launch_sweep_f64(prm(double{}), vw, g, v, grid, sms, s); break;
-    case Kind::F32C: launch_sweep_f32c(prm(float{}), vw, g, v, grid, sms, s); break;
-    case Kind::F32: launch_sweep_f32(prm(float{}), vw, g, v, grid, sms, s); break;
-    case Kind::F64S: launch_sweep_f64s(prm(DF{}), vw, g, v, grid, sms, s); break;
+    // A last column tile under a quarter full costs nearly a full pass at g lanes per row (its
+    // warps gather one or two edges per sub-step): it runs as a launch of its own with as few
+    // lanes per row as its columns need.
+    const long long vecs = (L.stride + L.vw - 1) / L.vw;
+    const long long full = vecs / sh.g, rem = vecs % sh.g;
+    if (full >= 1 && rem > 0 && rem * 4 <= sh.g && full + 1 <= ts && full + 1 == sh.ntiles) {
+        const int gr = static_cast<int>(next_pow2(rem));
+        launch(sh.g, static_cast<int>(full), sh.variant, 0, 0);
+        launch(gr, 1, 0, static_cast<int>(full * sh.g * L.vw), static_cast<int>(full));
+        return 2;
     }
+    launch(sh.g, sh.ntiles, sh.variant, 0, 0);
     return 1;
 }
 

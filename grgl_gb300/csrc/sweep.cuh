@@ -60,6 +60,9 @@ template <typename S> struct SweepParams {
     // Staged launches (sweep_kernel_staged): the `src_rows` single-element source rows from `src`
     // are copied into shared memory first and gathered from there; ids are relative to `src`.
     long long src_rows;
+    // First column of the launch's tile 0 (a launch of the last, narrow tile starts past the
+    // full tiles of another launch).
+    int col_base;
 };
 
 // Edge id e of a chunk as stored (32-bit, or 16-bit zero-extended).  The load is issued a step
@@ -252,7 +255,7 @@ __device__ __forceinline__ void sweep_chunk(const SweepParams<typename Op::S>& p
 
     const int lg = lane / G;  // group
     const int li = lane % G;  // lane inside the group
-    const int col = blockIdx.y * (G * VW) + li * VW;
+    const int col = p.col_base + blockIdx.y * (G * VW) + li * VW;
     const bool colok = col < p.stride;
     const unsigned upto = (2u << lg) - 1u;  // groups 0..lg
 

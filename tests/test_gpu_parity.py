@@ -147,7 +147,7 @@ def test_heavy_rows(gx, dtype):
     g = gx.from_csr(**arrs)
     og = oracle.OracleGraph(**arrs)
     rng = np.random.default_rng(2)
-    for K in (1, 4, 40):
+    for K in (1, 4, 40, 136):  # 136: a narrow last column tile, launched on its own
         for direction, cols in ((UP, og.num_samples), (DOWN, og.num_mutations)):
             V = (rng.standard_normal((K, cols)) if np.dtype(dtype).kind == "f"
                  else rng.integers(-9, 9, size=(K, cols))).astype(dtype)
