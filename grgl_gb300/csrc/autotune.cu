@@ -157,22 +157,21 @@ std::string autotune_impl(grgx_graph* g, int dtype, uint64_t rows, int direction
     };
     std::vector<std::vector<Pass>> forms;
     const long long h0 = static_cast<long long>(dp->level_begin.size() > 1 ? dp->level_begin[1] : 0);
+    // (on the chunking calls of this row width run on)
     if (down) {
-        forms.push_back({{&dp->down, 0, "level", 0, false}});
-        if (down_split_possible(dp)) {
-            ensure_down_split(g, dp);
-            if (dp->down0b.n_rows > 0)
-                forms.push_back({{&dp->down, 0, "split: level", 0, true},
-                                 {&dp->down0b, 1, "split: height-0 parent block", 0, false}});
-        }
+        if (down_split_possible(dp)) ensure_down_split(g, dp);
+        const SweepCSRs cs = sweep_csrs(dp, L);
+        forms.push_back({{cs.down, 0, "level", 0, false}});
+        if (cs.down0b->n_rows > 0)
+            forms.push_back({{cs.down, 0, "split: level", 0, true},
+                             {cs.down0b, 1, "split: height-0 parent block", 0, false}});
     } else {
-        forms.push_back({{&dp->up, 0, "level", 0, false}});
-        if (up_split_possible(dp)) {
-            ensure_up_split(g, dp);
-            if (dp->up0b.n_rows > 0)
-                forms.push_back({{&dp->up0b, 1, "split: height-0 block", dp->split_src, false},
-                                 {&dp->up_int, 2, "split: level", dp->split_src, false}});
-        }
+        if (up_split_possible(dp)) ensure_up_split(g, dp);
+        const SweepCSRs cs = sweep_csrs(dp, L);
+        forms.push_back({{cs.up, 0, "level", 0, false}});
+        if (cs.up0b->n_rows > 0)
+            forms.push_back({{cs.up0b, 1, "split: height-0 block", dp->split_src, false},
+                             {cs.up_int, 2, "split: level", dp->split_src, false}});
     }
     long long maxPieces = 0, maxHeavy = 0;
     for (const auto& f : forms)

@@ -396,7 +396,8 @@ extern "C" grgx_status grgx_graph_upload_host_plan(grgx_graph* g) {
 // chunks -- the stages the device builder shares), so that its invariants can be checked
 // without a GPU.  Names: "level_begin", "old2new", "new2old", "mut_new", "miss_new",
 // "down_row_of", and "<csr>.<field>" for csr in up/down/seed/miss and field in rows/off/adj/
-// chunks/heavy/level_chunk_begin/level_chunk_end.  The arrays stay valid until the graph is
+// chunks/heavy/level_chunk_begin/level_chunk_end (and up_fine/down_fine, the finer chunking of
+// up/down: chunks, heavy and the level ranges only).  The arrays stay valid until the graph is
 // destroyed.
 extern "C" grgx_status grgx_debug_host_plan(grgx_graph* g, const char* name, const void** data,
                                             uint64_t* bytes) {
@@ -421,7 +422,8 @@ extern "C" grgx_status grgx_debug_host_plan(grgx_graph* g, const char* name, con
         else if (n == "miss_new") put(p.miss_new);
         else if (n == "down_row_of") put(p.down_row_of);
         const std::pair<const char*, const grgx::PullCSR*> csrs[] = {
-            {"up.", &p.up}, {"down.", &p.down}, {"seed.", &p.seed}, {"miss.", &p.miss}};
+            {"up.", &p.up},           {"down.", &p.down},           {"seed.", &p.seed},
+            {"miss.", &p.miss},       {"up_fine.", &p.up_fine},     {"down_fine.", &p.down_fine}};
         for (const auto& c : csrs) {
             if (n.rfind(c.first, 0) != 0) continue;
             const std::string f = n.substr(std::string(c.first).size());

@@ -37,6 +37,9 @@ struct DevCSR {
 struct DevicePlan {
     int device = -1;
     DevCSR up, down, seed, miss;
+    // up / down (and below up0b, up_int, down0b) on the fine chunking: the same adjacency and
+    // rows, kFineChunkFactor times the chunks per level (sweep_csrs picks them for wide rows)
+    DevCSR up_f, down_f;
     // UP in split form (empty when the height-0 nodes make fewer than two blocks):
     //   up0b    the edges to height-0 children, cut by blocks of `split_block` height-0 ids;
     //           level j = block j, rows = every node with children in the block
@@ -45,7 +48,7 @@ struct DevicePlan {
     //           concatenated; fin_begin[j] .. fin_begin[j+1] for level j
     // Built on the first call that runs UP in split form (use_up_split), from the UP row offsets
     // and level boundaries kept here.
-    DevCSR up0b, up_int;
+    DevCSR up0b, up_int, up0b_f, up_int_f;
     int* fin = nullptr;
     std::vector<long long> fin_begin;
     long long split_block = 0, split_src = 0;  // split_src = height-0 ids = first UP row's node id
@@ -57,7 +60,7 @@ struct DevicePlan {
     //           every height-0 row with parents in the block; 16-bit block-relative ids
     //   fin_down the height-0 DOWN rows, finished from their state after the block passes
     // Built on the first call that runs DOWN in split form (use_down_split).
-    DevCSR down0b;
+    DevCSR down0b, down0b_f;
     int* fin_down = nullptr;
     long long n_fin_down = 0;
     bool down_split_built = false;
@@ -106,6 +109,23 @@ LevelShape level_shape(const Layout& L, const DevCSR& c, size_t level);
 // Column tiles of the widest shape the autotuner may pick for L: the stride of the per-launch
 // work counters and of the heavy-row tickets.
 int max_tiles(const Layout& L);
+
+// The sweep CSRs a call with layout L runs on: rows of 32 bytes or more (K >= 8 four-byte or
+// K >= 4 eight-byte values) take the fine chunking, narrower rows -- whose chunks cost little
+// each, so that more of them only adds per-chunk work (the staged single-column passes lose
+// 10-20%) -- the coarse one.  The split copies' members are empty until they are built.
+struct SweepCSRs {
+    const DevCSR* up;
+    const DevCSR* down;
+    const DevCSR* up0b;
+    const DevCSR* up_int;
+    const DevCSR* down0b;
+};
+bool fine_chunks(const Layout& L);
+SweepCSRs sweep_csrs(const DevicePlan* dp, const Layout& L);
+// `coarse` with the chunks, heavy rows and level ranges of `fine` (uploaded; the adjacency and
+// rows are shared).
+DevCSR fine_view(DevicePlan& d, const DevCSR& coarse, const PullCSR& fine);
 
 // Launches one level of a CSR (a no-op when the level has no chunks); `work` points at
 // `tileStride` (0: L.ntiles) zeroed counters owned by this launch, and the heavy-row tickets

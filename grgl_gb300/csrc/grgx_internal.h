@@ -111,6 +111,11 @@ struct HostPlan {
     PullCSR down;   // levels H..0 descending; rows = nodes with parents, adj = parents
                     // (adj left empty: built on the device from `up` by a stable sort)
     std::vector<int32_t> down_row_of;  // new id -> DOWN row (or -1)
+    // The same UP and DOWN rows and levels cut into kFineChunkFactor times as many chunks (only
+    // chunks, heavy rows and level ranges are filled): calls whose rows are wide enough for the
+    // per-chunk cost not to matter run on these (shorter tails at level ends, heavy rows in more
+    // pieces).
+    PullCSR up_fine, down_fine;
     PullCSR seed;   // one "level": rows = mutation nodes, adj = mutation ids
     PullCSR miss;   // one "level": rows = missingness nodes, adj = mutation ids
     std::vector<uint32_t> mut_new, miss_new;  // mutation -> new node id (or INVALID)
@@ -124,7 +129,13 @@ std::unique_ptr<HostPlan> build_plan(const HostGraph& g);
 // Stages of the plan shared by the host builder (build_plan) and the device builder
 // (plan_device.cu), which computes heights, the renumbering, the UP adjacency and the parent
 // counts on the GPU and lays out rows and chunks here.
-void chunk_level(PullCSR& P, const std::vector<int64_t>& off, int64_t rb, int64_t re);
+// Chunks rows rb..re-1 as one level, aiming at `target` chunks (0: chunk_target()).
+void chunk_level(PullCSR& P, const std::vector<int64_t>& off, int64_t rb, int64_t re, int64_t target = 0);
+// Finer chunking of the wide-row calls: this many times chunk_target() chunks per level.
+constexpr int64_t kFineChunkFactor = 4;
+// The levels of P (row offsets `off`) chunked again for `factor` times chunk_target() chunks per
+// level; the result holds chunks (with the sentinel), heavy rows, level ranges and piece count.
+PullCSR rechunk(const PullCSR& P, const std::vector<int64_t>& off, int64_t factor);
 // While alive, plans built on this thread size their chunks for a device with `sms` SMs.
 class PlanDeviceScope {
   public:

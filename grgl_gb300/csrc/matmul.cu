@@ -72,6 +72,24 @@ DevCSR upload_csr(DevicePlan& d, const PullCSR& c) {
 
 }  // namespace
 
+DevCSR fine_view(DevicePlan& d, const DevCSR& coarse, const PullCSR& fine) {
+    DevCSR r = coarse;
+    r.chunks = reinterpret_cast<ChunkDev*>(upload(d, fine.chunks));
+    r.heavy = reinterpret_cast<HeavyDev*>(upload(d, fine.heavy));
+    r.lb = fine.level_chunk_begin;
+    r.le = fine.level_chunk_end;
+    r.n_heavy = static_cast<long long>(fine.heavy.size());
+    r.n_pieces = fine.num_pieces;
+    return r;
+}
+
+bool fine_chunks(const Layout& L) { return L.stride * L.ssize >= 32; }
+
+SweepCSRs sweep_csrs(const DevicePlan* dp, const Layout& L) {
+    if (fine_chunks(L)) return SweepCSRs{&dp->up_f, &dp->down_f, &dp->up0b_f, &dp->up_int_f, &dp->down0b_f};
+    return SweepCSRs{&dp->up, &dp->down, &dp->up0b, &dp->up_int, &dp->down0b};
+}
+
 // The library's own stream-ordered pool on `device` (created once per device; the process's
 // default pool, which the host application may use too, is left as it is).  Memory freed into it
 // stays cached for the next call (release threshold: never).  Calls on different streams are not
@@ -419,6 +437,8 @@ DevicePlan* ensure_device_plan_once(grgx_graph* g) {
         d->allocs.push_back(d->down.adj);
         d->bytes += static_cast<uint64_t>(hp.down.num_edges) * sizeof(uint32_t);
     }
+    d->up_f = fine_view(*d, d->up, hp.up_fine);
+    d->down_f = fine_view(*d, d->down, hp.down_fine);
     d->seed = upload_csr(*d, hp.seed);
     d->miss = upload_csr(*d, hp.miss);
     d->mut_new = upload(*d, hp.mut_new);
@@ -571,17 +591,24 @@ void matmul_direct(grgx_graph* g, int dtype, const void* input, uint64_t in_cols
         const bool split = !down && use_up_split(g, dp, L);
         // DOWN in split form: the height-0 level in parent blocks (up_split.cu)
         const bool dsplit = down && use_down_split(g, dp, L);
-        long long pieces = down ? std::max(dp->down.n_pieces, std::max(dp->seed.n_pieces, dp->miss.n_pieces))
-                                : (split ? std::max(dp->up0b.n_pieces, dp->up_int.n_pieces) : dp->up.n_pieces);
-        if (dsplit) pieces = std::max(pieces, dp->down0b.n_pieces);
+        // coarse or fine chunking for this row width (the split copies are built by now)
+        const SweepCSRs cs = sweep_csrs(dp, L);
+        const DevCSR& cUp = *cs.up;
+        const DevCSR& cDown = *cs.down;
+        const DevCSR& cUp0b = *cs.up0b;
+        const DevCSR& cUpInt = *cs.up_int;
+        const DevCSR& cDown0b = *cs.down0b;
+        long long pieces = down ? std::max(cDown.n_pieces, std::max(dp->seed.n_pieces, dp->miss.n_pieces))
+                                : (split ? std::max(cUp0b.n_pieces, cUpInt.n_pieces) : cUp.n_pieces);
+        if (dsplit) pieces = std::max(pieces, cDown0b.n_pieces);
         void* partials = sc.get(static_cast<size_t>(pieces) * L.stride * L.asize);
-        const long long nh = down ? (dp->down.n_heavy + dp->seed.n_heavy + dp->miss.n_heavy +
-                                     (dsplit ? dp->down0b.n_heavy : 0))
-                                  : (split ? dp->up0b.n_heavy + dp->up_int.n_heavy : dp->up.n_heavy);
-        const long long nslots = down ? (2 + static_cast<long long>(dp->down.lb.size()) +
-                                         (dsplit ? static_cast<long long>(dp->down0b.lb.size()) : 0))
-                                      : static_cast<long long>(split ? dp->up0b.lb.size() + dp->up_int.lb.size()
-                                                                     : dp->up.lb.size());
+        const long long nh = down ? (cDown.n_heavy + dp->seed.n_heavy + dp->miss.n_heavy +
+                                     (dsplit ? cDown0b.n_heavy : 0))
+                                  : (split ? cUp0b.n_heavy + cUpInt.n_heavy : cUp.n_heavy);
+        const long long nslots = down ? (2 + static_cast<long long>(cDown.lb.size()) +
+                                         (dsplit ? static_cast<long long>(cDown0b.lb.size()) : 0))
+                                      : static_cast<long long>(split ? cUp0b.lb.size() + cUpInt.lb.size()
+                                                                     : cUp.lb.size());
         const long long h0 = static_cast<long long>(dp->level_begin.size() > 1 ? dp->level_begin[1] : 0);
         const size_t stateBytes = split    ? static_cast<size_t>(n - dp->split_src) * L.stride * std::max(L.asize, 8)
                                   : dsplit ? static_cast<size_t>(h0) * L.stride * std::max(L.asize, 8)
@@ -691,20 +718,20 @@ void matmul_direct(grgx_graph* g, int dtype, const void* input, uint64_t in_cols
                 }
                 tk += dp->miss.n_heavy * TS;
                 if (timed && t_timing) GRGX_CUDA(cudaEventRecord(ev[1], s));
-                const size_t nlv = dp->down.lb.size();
+                const size_t nlv = cDown.lb.size();
                 for (size_t lvl = 0; lvl < nlv; lvl++) {
                     if (dsplit && lvl + 1 == nlv) break;  // the height-0 level runs in split form below
-                    launches += level(dp->down, lvl, vals, 1, tk, work + (2 + lvl) * TS);
+                    launches += level(cDown, lvl, vals, 1, tk, work + (2 + lvl) * TS);
                 }
                 if (dsplit) {
                     // parent-block passes merge each height-0 row's sums into its state; then the
                     // rows are written from it, onto their seed / init values
                     GRGX_CUDA(cudaMemsetAsync(state, 0, stateBytes, s));
-                    unsigned* tS = tk + dp->down.n_heavy * TS;
+                    unsigned* tS = tk + cDown.n_heavy * TS;
                     unsigned* wS = work + (2 + nlv) * TS;
-                    for (size_t j = 0; j < dp->down0b.lb.size(); j++) {
-                        const LevelShape sh = level_shape(LL, dp->down0b, j);
-                        launches += launch_level(LL, dp->down0b, j, vals, vals, 0, partials, tS, wS + j * TS, s, g,
+                    for (size_t j = 0; j < cDown0b.lb.size(); j++) {
+                        const LevelShape sh = level_shape(LL, cDown0b, j);
+                        launches += launch_level(LL, cDown0b, j, vals, vals, 0, partials, tS, wS + j * TS, s, g,
                                                  gv, &sh, TS, state, 0, 1);
                     }
                     launch_state_finish(LL.kind, state, vals, dp->fin_down, dp->n_fin_down, 0, LL.stride, 1, s, g,
@@ -726,18 +753,18 @@ void matmul_direct(grgx_graph* g, int dtype, const void* input, uint64_t in_cols
                 if (split) {
                     GRGX_CUDA(cudaMemsetAsync(state, 0, stateBytes, s));
                     unsigned* t0b = tickets;
-                    unsigned* tIn = tickets + dp->up0b.n_heavy * TS;
+                    unsigned* tIn = tickets + cUp0b.n_heavy * TS;
                     unsigned* w0b = work;
-                    unsigned* wIn = work + dp->up0b.lb.size() * TS;
+                    unsigned* wIn = work + cUp0b.lb.size() * TS;
                     const long long base = dp->split_src;
-                    for (size_t j = 0; j < dp->up0b.lb.size(); j++) {
-                        const LevelShape sh = level_shape(LL, dp->up0b, j);
-                        launches += launch_level(LL, dp->up0b, j, vals, vals, 0, partials, t0b, w0b + j * TS, s, g,
+                    for (size_t j = 0; j < cUp0b.lb.size(); j++) {
+                        const LevelShape sh = level_shape(LL, cUp0b, j);
+                        launches += launch_level(LL, cUp0b, j, vals, vals, 0, partials, t0b, w0b + j * TS, s, g,
                                                  gv, &sh, TS, state, base, 1);
                     }
-                    for (size_t lvl = 0; lvl < dp->up_int.lb.size(); lvl++) {
-                        const LevelShape sh = level_shape(LL, dp->up_int, lvl);
-                        launches += launch_level(LL, dp->up_int, lvl, vals, vals, hasInit, partials, tIn,
+                    for (size_t lvl = 0; lvl < cUpInt.lb.size(); lvl++) {
+                        const LevelShape sh = level_shape(LL, cUpInt, lvl);
+                        launches += launch_level(LL, cUpInt, lvl, vals, vals, hasInit, partials, tIn,
                                                  wIn + lvl * TS, s, g, gv, &sh, TS, state, base, 2);
                         const long long f0 = dp->fin_begin[lvl], f1 = dp->fin_begin[lvl + 1];
                         if (f1 > f0) {
@@ -747,8 +774,8 @@ void matmul_direct(grgx_graph* g, int dtype, const void* input, uint64_t in_cols
                         }
                     }
                 } else {
-                    for (size_t lvl = 0; lvl < dp->up.lb.size(); lvl++)
-                        launches += level(dp->up, lvl, vals, hasInit, tickets, work + lvl * TS);
+                    for (size_t lvl = 0; lvl < cUp.lb.size(); lvl++)
+                        launches += level(cUp, lvl, vals, hasInit, tickets, work + lvl * TS);
                 }
                 if (timed && t_timing) GRGX_CUDA(cudaEventRecord(ev[2], s));
                 if (emit_all) {

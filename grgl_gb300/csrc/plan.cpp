@@ -62,11 +62,11 @@ PlanDeviceScope::~PlanDeviceScope() { t_plan_sms = saved_; }
 
 int64_t chunk_target() { return static_cast<int64_t>(t_plan_sms > 0 ? t_plan_sms : kHostOnlySms) * 16 * 8; }
 
-void chunk_level(PullCSR& P, const std::vector<int64_t>& off, int64_t rb, int64_t re) {
+void chunk_level(PullCSR& P, const std::vector<int64_t>& off, int64_t rb, int64_t re, int64_t target) {
     P.level_chunk_begin.push_back(static_cast<int32_t>(P.chunks.size()));
     const int64_t levelEdges = off[re] - off[rb];
     P.max_level_edges = std::max(P.max_level_edges, levelEdges);
-    const int64_t target = chunk_target();
+    if (target <= 0) target = chunk_target();
     int64_t C = (levelEdges + target - 1) / target;
     C = ((C + 31) / 32) * 32;
     C = std::max(kMinChunk, std::min(kMaxChunk, C));
@@ -98,6 +98,20 @@ void chunk_level(PullCSR& P, const std::vector<int64_t>& off, int64_t rb, int64_
         P.chunks.push_back(Chunk{off[r0], static_cast<int32_t>(r0), -1});
     }
     P.level_chunk_end.push_back(static_cast<int32_t>(P.chunks.size()));
+}
+
+PullCSR rechunk(const PullCSR& P, const std::vector<int64_t>& off, int64_t factor) {
+    PullCSR Q;
+    const int64_t target = chunk_target() * factor;
+    for (size_t l = 0; l < P.level_chunk_begin.size(); l++) {
+        // a level's rows: from its first chunk's row to the next level's (or the sentinel's)
+        const int64_t rb = P.chunks[static_cast<size_t>(P.level_chunk_begin[l])].r0;
+        const int64_t re = P.chunks[static_cast<size_t>(P.level_chunk_end[l])].r0;
+        chunk_level(Q, off, rb, re, target);
+    }
+    Q.chunks.push_back(Chunk{off.empty() ? 0 : off.back(), static_cast<int32_t>(P.rows.size()), -1});
+    Q.num_edges = P.num_edges;
+    return Q;
 }
 
 void finish_csr(PullCSR& P, const std::vector<int64_t>& off) {
@@ -160,6 +174,7 @@ void plan_up_layout(HostPlan& plan, std::vector<int64_t> off) {
         chunk_level(P, off, static_cast<int64_t>(plan.level_begin[h] - r0),
                     static_cast<int64_t>(plan.level_begin[h + 1] - r0));
     finish_csr(P, off);
+    plan.up_fine = rechunk(P, off, kFineChunkFactor);
     P.off = std::move(off);
 }
 
@@ -191,6 +206,7 @@ void plan_down_layout(HostPlan& plan, const std::vector<uint64_t>& pdeg) {
         rb = re;
     }
     finish_csr(P, off);
+    plan.down_fine = rechunk(P, off, kFineChunkFactor);
     P.off = std::move(off);
 }
 

@@ -219,11 +219,13 @@ void launch_state_finish(Kind kind, const void* state, void* vals, const int* no
 namespace {
 // Block-major rows of the block passes from the per-row segment boundaries `seg` (R rows, nb+1
 // entries each): level b = the rows with edges in block b; dst0[i*nb + b] = where row i's
-// segment b starts in the copy.  Returns the copy's edge count.
+// segment b starts in the copy; off0 = the copy's row offsets.  Returns the copy's edge count.
 long long block_layout(PullCSR& P0, const std::vector<uint32_t>& seg, long long R, int nb,
-                       const std::function<int32_t(long long)>& nodeOf, std::vector<long long>& dst0) {
+                       const std::function<int32_t(long long)>& nodeOf, std::vector<long long>& dst0,
+                       std::vector<int64_t>& off0) {
     auto S = [&](long long i, int b) { return static_cast<long long>(seg[static_cast<size_t>(i) * (nb + 1) + b]); };
-    std::vector<int64_t> off0(1, 0), rowBegin0;
+    std::vector<int64_t> rowBegin0;
+    off0.assign(1, 0);
     dst0.assign(static_cast<size_t>(R) * nb, 0);
     for (int b = 0; b < nb; b++) {
         rowBegin0.push_back(static_cast<int64_t>(P0.rows.size()));
@@ -280,8 +282,9 @@ void build_up_split(DevicePlan& d) {
         // height-0 passes: block-major rows
         PullCSR P0;
         std::vector<long long> dst0;
+        std::vector<int64_t> off0;
         const long long E0 = block_layout(P0, seg, R, nb, [&](long long i) { return static_cast<int32_t>(src0 + i); },
-                                          dst0);
+                                          dst0, off0);
 
         // internal edges: one level per UP level (heights 1..H-1), plus the finish lists
         PullCSR PI;
@@ -337,6 +340,8 @@ void build_up_split(DevicePlan& d) {
         }
         d.up0b = upload_pull(d, P0, a0, E0, &base, &rows);
         d.up_int = upload_pull(d, PI, aI, EI);
+        d.up0b_f = fine_view(d, d.up0b, rechunk(P0, off0, kFineChunkFactor));
+        d.up_int_f = fine_view(d, d.up_int, rechunk(PI, offI, kFineChunkFactor));
         if (!fin.empty()) {
             void* p = nullptr;
             BL_CUDA(cudaMalloc(&p, fin.size() * sizeof(int)));
@@ -402,8 +407,9 @@ void build_down_split(DevicePlan& d) {
                        GRGX_ERR_CUDA, "height-0 row with a parent of height 0");
         PullCSR P0;
         std::vector<long long> dst0;
+        std::vector<int64_t> off0;
         const long long E0 = block_layout(P0, seg, R, nb, [&](long long i) { return rowNode[static_cast<size_t>(i)]; },
-                                          dst0);
+                                          dst0, off0);
         GRGX_CHECK(E0 == E, GRGX_ERR_CUDA, "split edge count mismatch");
         long long* dDst0 = static_cast<long long*>(dmalloc(dst0.size() * sizeof(long long)));
         BL_CUDA(cudaMemcpy(dDst0, dst0.data(), dst0.size() * sizeof(long long), cudaMemcpyHostToDevice));
@@ -424,6 +430,7 @@ void build_down_split(DevicePlan& d) {
             rows[b] = std::min(block, n - base[b]);
         }
         d.down0b = upload_pull(d, P0, a0, E0, &base, &rows);
+        d.down0b_f = fine_view(d, d.down0b, rechunk(P0, off0, kFineChunkFactor));
         void* p = nullptr;
         BL_CUDA(cudaMalloc(&p, rowNode.size() * sizeof(int)));
         d.allocs.push_back(p);

@@ -86,6 +86,17 @@ def check_chunks(csr, off, level_rows):
                           if len(heavy) else heavy["slot_base"])
 
 
+def check_fine(fine, coarse, off, level_rows):
+    """The finer chunking of the same rows: the same levels, every edge once, and at least as many
+    chunks per level as the coarse chunking."""
+    check_chunks(fine, off, level_rows)
+    for l, (rb, re) in enumerate(level_rows):
+        nc = coarse["level_chunk_end"][l] - coarse["level_chunk_begin"][l]
+        nf = fine["level_chunk_end"][l] - fine["level_chunk_begin"][l]
+        assert nf >= nc
+    assert len(fine["chunks"]) >= len(coarse["chunks"])
+
+
 def check_plan(g):
     a = g.export_arrays()
     n, N = g.num_nodes, g.num_samples
@@ -96,6 +107,8 @@ def check_plan(g):
     for c in ("up", "down", "seed", "miss"):
         P[c] = {f: plan_array(g, f"{c}.{f}") for f in ("rows", "off", "adj", "chunks", "heavy",
                                                        "level_chunk_begin", "level_chunk_end")}
+    for c in ("up_fine", "down_fine"):
+        P[c] = {f: plan_array(g, f"{c}.{f}") for f in ("chunks", "heavy", "level_chunk_begin", "level_chunk_end")}
     lb = P["level_begin"].astype(np.int64)
     assert len(lb) == L + 1 and np.array_equal(np.diff(lb), np.bincount(h, minlength=L))
     o2n, n2o = P["old2new"].astype(np.int64), P["new2old"].astype(np.int64)
@@ -121,6 +134,7 @@ def check_plan(g):
         old = n2o[up["rows"][i]]
         assert np.array_equal(kids[s:e], o2n[adj[off[old]:off[old + 1]].astype(np.int64)])
     check_chunks(up, up["off"], [(lb[k] - r0, lb[k + 1] - r0) for k in range(1, L)])
+    check_fine(P["up_fine"], up, up["off"], [(lb[k] - r0, lb[k + 1] - r0) for k in range(1, L)])
 
     # DOWN: nodes with parents, heights descending, ids ascending inside a height
     dn = P["down"]
@@ -138,6 +152,7 @@ def check_plan(g):
         levels.append((pos, pos + cnt))
         pos += cnt
     check_chunks(dn, dn["off"], levels)
+    check_fine(P["down_fine"], dn, dn["off"], levels)
 
     # seeds: mutation -> new node, rows = mapped nodes ascending, mutation ids ascending per row
     mut = a["mut_node"].astype(np.int64)
@@ -181,3 +196,25 @@ def test_host_plan_of_window_tree(lib_built):
     import grgl_gb300 as gx
 
     check_plan(gx.window_tree_grg(3000, 20000, seed=13))
+
+
+def test_host_plan_fine_chunks(lib_built):
+    """A level with millions of edges: the fine chunking cuts it into several times the coarse
+    chunking's chunks (heavy rows into more pieces), and both cover every edge once."""
+    import grgl_gb300 as gx
+
+    N, rows, deg = 40_000, 100, 40_000
+    rng = np.random.default_rng(4)
+    children = [np.sort(rng.choice(N, size=deg, replace=False)) for _ in range(rows)]
+    off = np.concatenate([np.zeros(N + 1, np.uint64), np.cumsum([len(c) for c in children]).astype(np.uint64)])
+    adj = np.concatenate(children).astype(np.uint32)
+    g = gx.from_csr(num_samples=N, ploidy=2, down_off=off, down_adj=adj,
+                    mut_node=np.arange(N, N + rows, dtype=np.uint32))
+    up = {f: plan_array(g, f"up.{f}") for f in ("rows", "off", "chunks", "heavy", "level_chunk_begin",
+                                                 "level_chunk_end")}
+    fine = {f: plan_array(g, f"up_fine.{f}") for f in ("chunks", "heavy", "level_chunk_begin", "level_chunk_end")}
+    levels = [(0, rows)]
+    check_chunks(up, up["off"], levels)
+    check_fine(fine, up, up["off"], levels)
+    assert len(fine["chunks"]) > 2 * len(up["chunks"])
+    assert fine["heavy"]["n_pieces"].sum() > 2 * up["heavy"]["n_pieces"].sum()
