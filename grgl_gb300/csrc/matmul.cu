@@ -384,8 +384,10 @@ cudaError_t pool_malloc(void** p, size_t bytes, cudaStream_t s) {
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     if (cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return e;
     cudaGetLastError();
-    const cudaError_t se = cudaDeviceSynchronize();
-    if (se != cudaSuccess) return se;
+    // let pending frees complete, then try once more (the synchronisation itself may be refused
+    // while another thread captures a CUDA graph: the retry then sees what has completed)
+    cudaDeviceSynchronize();
+    cudaGetLastError();
     return cudaMallocFromPoolAsync(p, bytes, pool, s);
 }
 
@@ -916,21 +918,31 @@ void matmul_impl(grgx_graph* g, int dtype, const void* input, uint64_t in_cols, 
                       ent->stream);
         GRGX_CUDA(cudaStreamSynchronize(ent->stream));
         cudaGraph_t graph = nullptr;
-        GRGX_CUDA(cudaStreamBeginCapture(ent->stream, cudaStreamCaptureModeThreadLocal));
-        try {
-            matmul_direct(g, dtype, ent->in, in_cols, rows, direction, ent->out, output_size, emit_all, by_indiv,
-                          init_kind == GRGX_INIT_VECTOR || init_kind == GRGX_INIT_MATRIX ? ent->init : init, init_kind,
-                          useMiss ? ent->miss : nullptr,
-                          (flags | GRGX_FLAG_DEVICE_POINTERS | GRGX_FLAG_NO_GRAPH) & ~GRGX_FLAG_SYNC, ent->stream);
-        } catch (...) {
-            cudaStreamEndCapture(ent->stream, &graph);
+        bool captured = false;
+        if (cudaStreamBeginCapture(ent->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+            bool ok = true;
+            try {
+                matmul_direct(g, dtype, ent->in, in_cols, rows, direction, ent->out, output_size, emit_all, by_indiv,
+                              init_kind == GRGX_INIT_VECTOR || init_kind == GRGX_INIT_MATRIX ? ent->init : init,
+                              init_kind, useMiss ? ent->miss : nullptr,
+                              (flags | GRGX_FLAG_DEVICE_POINTERS | GRGX_FLAG_NO_GRAPH) & ~GRGX_FLAG_SYNC, ent->stream);
+            } catch (...) {
+                ok = false;
+            }
+            const cudaError_t ee = cudaStreamEndCapture(ent->stream, &graph);
+            captured = ok && ee == cudaSuccess && graph != nullptr &&
+                       cudaGraphInstantiate(&ent->exec, graph, 0) == cudaSuccess;
             if (graph) cudaGraphDestroy(graph);
-            throw;
         }
-        GRGX_CUDA(cudaStreamEndCapture(ent->stream, &graph));
-        const cudaError_t ie = cudaGraphInstantiate(&ent->exec, graph, 0);
-        cudaGraphDestroy(graph);
-        GRGX_CUDA(ie);
+        if (!captured) {
+            // The capture failed -- another thread's device-wide operation (a synchronisation, a
+            // free that synchronises) invalidates a capture in progress: this call runs directly
+            // and a later call of the same shape captures again.
+            cudaGetLastError();
+            matmul_direct(g, dtype, input, in_cols, rows, direction, output, output_size, emit_all, by_indiv, init,
+                          init_kind, miss, flags | GRGX_FLAG_NO_GRAPH, stream_ptr);
+            return;
+        }
         std::lock_guard<std::mutex> lk(g->graphs->mu);
         auto it = g->graphs->entries.find(key);
         if (it != g->graphs->entries.end()) {

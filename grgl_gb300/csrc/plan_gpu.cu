@@ -103,7 +103,9 @@ uint32_t* build_down_adj_device(const uint32_t* upAdj, const int* upRows, const 
         result = vals.Current();
         set_heads_kernel<<<sm_count() * 8, 256>>>(result, dOff, R);
         PLAN_CUDA(cudaGetLastError());
-        PLAN_CUDA(cudaDeviceSynchronize());
+        // the sort and the kernels ran on the legacy stream: wait for that stream only (a
+        // device-wide synchronisation fails while another thread captures a CUDA graph)
+        PLAN_CUDA(cudaStreamSynchronize(cudaStreamLegacy));
     } catch (...) {
         for (void* p : temps) cudaFree(p);
         throw;

@@ -324,7 +324,7 @@ void build_up_split(DevicePlan& d) {
         BL_CUDA(cudaMalloc(reinterpret_cast<void**>(&outI), (EI ? EI : 1) * sizeof(uint32_t)));
         scatter_kernel<<<blocks_for(R, 8), 256>>>(d.up.adj, dOff, R, nb, block, 0, dSeg, dDst0, dDstI, out0, outI);
         BL_CUDA(cudaGetLastError());
-        BL_CUDA(cudaDeviceSynchronize());
+        BL_CUDA(cudaStreamSynchronize(cudaStreamLegacy));  // the legacy-stream kernels above, not the device
         freeTmp();
         void* a0 = out0;
         uint32_t* aI = outI;
@@ -418,7 +418,7 @@ void build_down_split(DevicePlan& d) {
         scatter_kernel<<<blocks_for(R, 8), 256>>>(adj, dOff, R, nb, block, src0, dSeg, dDst0, nullptr, out0,
                                                   nullptr);
         BL_CUDA(cudaGetLastError());
-        BL_CUDA(cudaDeviceSynchronize());
+        BL_CUDA(cudaStreamSynchronize(cudaStreamLegacy));  // the legacy-stream kernels above, not the device
         freeTmp();
         void* a0 = out0;
         d.allocs.push_back(a0);
