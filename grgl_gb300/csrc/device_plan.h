@@ -110,13 +110,10 @@ LevelShape level_shape(const Layout& L, const DevCSR& c, size_t level);
 // work counters and of the heavy-row tickets.
 int max_tiles(const Layout& L);
 
-// The sweep CSRs a call with layout L runs on: rows of 32 to 512 bytes (K = 8..128 four-byte or
-// K = 4..64 eight-byte values) take the fine chunking.  Narrower rows keep the coarse one: their
-// chunks cost little each, so that more of them only adds per-chunk work (the staged
-// single-column passes lose 10-20%).  So do wider ones, whose heavy rows would be cut into
-// more pieces than their finish can absorb (float32 K=256 on a 1M-sample graph: UP 172 -> 192
-// ms, DOWN 154 -> 162 ms on the fine chunking).  The split copies' members are empty until they
-// are built.
+// The sweep CSRs a call with layout L runs on: rows of 32 bytes or more (K >= 8 four-byte or
+// K >= 4 eight-byte values) take the fine chunking, narrower rows -- whose chunks cost little
+// each, so that more of them only adds per-chunk work (the staged single-column passes lose
+// 10-20%) -- the coarse one.  The split copies' members are empty until they are built.
 struct SweepCSRs {
     const DevCSR* up;
     const DevCSR* down;

@@ -83,10 +83,7 @@ DevCSR fine_view(DevicePlan& d, const DevCSR& coarse, const PullCSR& fine) {
     return r;
 }
 
-bool fine_chunks(const Layout& L) {
-    const long long rowBytes = L.stride * L.ssize;
-    return rowBytes >= 32 && rowBytes <= 512;
-}
+bool fine_chunks(const Layout& L) { return L.stride * L.ssize >= 32; }
 
 SweepCSRs sweep_csrs(const DevicePlan* dp, const Layout& L) {
     if (fine_chunks(L)) return SweepCSRs{&dp->up_f, &dp->down_f, &dp->up0b_f, &dp->up_int_f, &dp->down0b_f};
