@@ -169,18 +169,21 @@ def test_init_failures(gx, t200):
 
 
 def test_parallel(gx, t200):
-    """Range shards multiplied from four threads at once sum to the whole graph's DOWN product."""
+    """Range shards multiplied from four threads at once sum to the whole graph's DOWN product.
+    Each round takes fresh shards, so the threads' first calls -- device plans built on the
+    legacy stream, CUDA graphs captured on others -- overlap every time."""
     from grgl_gb300.shard import split_by_mutations
 
     g, _ = t200
-    V = np.random.default_rng(45).standard_normal((10, g.num_mutations))
-    full = gx.matmul(g, V, gx.DOWN)
-    ranges, shards = split_by_mutations(g, 4)
-    assert sum(s.num_mutations for s in shards) == g.num_mutations
-    with concurrent.futures.ThreadPoolExecutor(max_workers=4) as ex:
-        futures = [ex.submit(gx.matmul, s, V[:, r.start:r.stop], gx.DOWN) for s, r in zip(shards, ranges)]
-        parts = [f.result() for f in futures]
-    np.testing.assert_allclose(full, np.sum(parts, axis=0))
+    for rnd in range(5):
+        V = np.random.default_rng(45 + rnd).standard_normal((10, g.num_mutations))
+        full = gx.matmul(g, V, gx.DOWN)
+        ranges, shards = split_by_mutations(g, 4)
+        assert sum(s.num_mutations for s in shards) == g.num_mutations
+        with concurrent.futures.ThreadPoolExecutor(max_workers=4) as ex:
+            futures = [ex.submit(gx.matmul, s, V[:, r.start:r.stop], gx.DOWN) for s, r in zip(shards, ranges)]
+            parts = [f.result() for f in futures]
+        np.testing.assert_allclose(full, np.sum(parts, axis=0))
 
 
 # ---- test/endtoend/test_missing.py -------------------------------------------------------------
