@@ -228,8 +228,9 @@ SweepParams<S> make_params(const DevCSR& c, long long cb, long long ce, const vo
     return p;
 }
 
-// Launches one level of a CSR; returns the number of kernels launched (0 or 1).
-// `work` points at L.ntiles zeroed counters owned by this launch.
+// Launches one level of a CSR; returns the number of kernels launched (0, 1, or 2 when a nearly
+// empty last column tile runs on its own).  `work` points at `tileStride` zeroed counters owned
+// by this level.
 int launch_level(const Layout& L, const DevCSR& c, size_t level, const void* src, void* dst, int rmw,
                  void* partials, unsigned* tickets, unsigned* work, cudaStream_t s, const int* gate,
                  int gateValue, const LevelShape* shape, int tileStride, void* state, long long stateBase,
