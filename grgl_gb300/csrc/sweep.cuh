@@ -315,8 +315,22 @@ __device__ __forceinline__ void sweep_chunk(const SweepParams<typename Op::S>& p
                     for (int i = 0; i < VW; i++) v[u][i] = S{};
                 }
             }
-            if (anyHead == 0u) {
-                // no row starts in this step: every edge continues the current row
+            // No row starts in this batch of sub-steps: every edge continues the current row.  The
+            // step's heads are tested first (one test when the step has none); a boundary elsewhere
+            // in the step leaves this batch on the block path too, which adds its edges with fewer
+            // compensated additions and runs the short, shared code -- per-sub-step boundary code
+            // for every sub-step of a boundary step made UP split passes wait on instruction fetch.
+            auto batch_heads = [&]() {
+                unsigned bh = 0u;
+#pragma unroll
+                for (int u = 0; u < BATCH; u++) {
+                    const int t = t0 + u;
+                    const int b = t / G, s = t % G;
+                    bh |= (NG == 32) ? heads[b] : ((heads[b] >> (s * NG)) & NGMASK);
+                }
+                return bh;
+            };
+            if (anyHead == 0u || batch_heads() == 0u) {
                 acc.template add_block<BATCH>(v);
                 continue;
             }
