@@ -48,10 +48,11 @@ void parallel_for(uint64_t n, const std::function<void(uint64_t, uint64_t, int)>
 
 }  // namespace
 
-// Chunk target: enough chunks per level to give every SM several waves of warps (16 warps per
-// SM, 8 chunks each), never fewer than 64 edges per chunk.  The SM count is that of the device
-// the plan is built for (PlanDeviceScope); a plan built with no device in view (host-side
-// inspection) assumes a GB300's 152 SMs.
+// Chunk target (the coarse chunking): SMs x 128 chunks per level -- about four per resident warp
+// of the sweep kernel (32 warps per SM) -- never fewer than 64 edges per chunk; the fine chunking
+// aims at kFineChunkFactor times as many.  The SM count is that of the device the plan is built
+// for (PlanDeviceScope); a plan built with no device in view (host-side inspection) assumes a
+// GB300's 152 SMs.
 constexpr int64_t kMinChunk = 64;
 constexpr int64_t kMaxChunk = 1 << 22;
 constexpr int kHostOnlySms = 152;
